@@ -1,0 +1,192 @@
+// sph_device.cuh — device-side types and math shared by the GB300 SPH kernels.
+//
+// Layout in HBM (one "scene table" entry per independent simulation; a single-scene
+// handle is a table of one):
+//   sorted state S (double-buffered, S <-> S' each step), index = position in
+//   (cell, id) order:  x, v (double2 in 2D, double4 in 3D, w unused), rho, p, c,
+//   P = p / rho^2, mass, gap, T, kappa, cp, id, scene
+//   step outputs N (unsorted, same index as S): x', v', T', rho'
+//   cell list: count[cells], start[cells + 1] (exclusive scan), key/slot per particle
+//   walls (static, sorted once by (cell, wall index) on the host): x, normal, gap, T,
+//   kappa, v, kind, wall_start[cells + 1]
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+#include <stdint.h>
+
+#include "../../include/ethersph_gpu.h"
+
+namespace sph {
+
+constexpr int32_t kDeadKey = 0x7fffffff;
+
+// Status bits written by kernels (atomicOr) and read by the host after a step.
+enum : int32_t { kStatusNonFinite = 1, kStatusClamped = 2 };
+
+// Per-scene constants.  Every derived constant is formed on the host with the same
+// IEEE operation sequence the Julia code would use at the point of use, so using the
+// constant inside a kernel rounds exactly like recomputing it there.
+struct SceneDev {
+    // cell grid
+    double lo[3];
+    double inv_cell[3];
+    int32_t n[3];
+    int32_t cell_off;   // first global cell of this scene
+    int32_t ncells;
+    int32_t periodic_x;
+    double period;      // domain_hi[0] - domain_lo[0]
+    double half_period; // 0.5 * period
+    double wrap_hi;     // lo[0] + period
+
+    // SmoothKernel
+    double h, sigma, k0, rc2;
+    double kw_a;   // CubicSpline: sigma/4; Gaussian: sigma; WendlandC2: sigma; WendlandC4: sigma
+    double kg_a;   // gradient prefactor (see kernel_wdw)
+    double hh001;  // 0.01 * (h * h)
+
+    // model
+    double rho0, c0, p0, b, nu0, t0, cp, beta, P_bg;  // P_bg = p0 / (rho0 * rho0)
+    double inv_cp_d;  // 1.0 / cp
+    double g[3];
+    double bous[3];  // -g[k] * beta (Boussinesq prefactor)
+    int32_t gamma;
+    int32_t thermal;
+    int32_t wall_pressure;
+    int32_t uniform_gap;
+    int32_t check_enabled;
+    int32_t nan_check;
+    double dt, dt2half_unused;
+    double dtdt;     // dt * dt
+    int64_t reinit_interval;
+    int64_t check_interval;
+    double check_lo[3];
+    double check_hi[3];
+    double two_pi_unused;
+
+    // FP32-compensated form
+    float cell_f[3];   // cell edge per axis (float)
+    float h_f, rc2_f, hh001_f, nu0_f, P_bg_f;
+    float kw_a_f, kg_a_f, inv_h_f, c0_f, rho0_f, inv_cp_f, inv_rho0_f;
+    float pad_f[3];
+};
+
+// ---------------------------------------------------------------- vector types
+template <int DIM> struct VecT;
+template <> struct VecT<2> { using T = double2; };
+template <> struct VecT<3> { using T = double4; };
+
+template <int DIM> struct FVec;
+template <> struct FVec<2> { using T = float2; };
+template <> struct FVec<3> { using T = float4; };
+
+__device__ __forceinline__ double comp(const double2& a, int k) { return k == 0 ? a.x : a.y; }
+__device__ __forceinline__ double comp(const double4& a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+// ---------------------------------------------------------------- state buffers
+struct SortedState {
+    void* x;
+    void* v;
+    double* rho;   // density at the start of the step
+    double* rhoc;  // density after the continuity update (K4 output)
+    double* p;
+    double* c;
+    double* P;
+    double* m;
+    double* gap;
+    double* T;
+    double* kappa;
+    double* cp;
+    int32_t* id;
+    int32_t* scene;
+    // FP32 shadows (allocated only for the compensated form)
+    float4* fa;   // 2D: (xr, yr, vx, vy)      3D: (xr, yr, zr, m)
+    float4* fb;   // 2D: (m, rho, P, gap)      3D: (vx, vy, vz, rho)
+    float4* fc;   // 2D: (T, kappa, cp, -)     3D: (P, gap, T, kappa)
+    float* fd;    // 3D: cp
+    int32_t* cell;  // cell key of the particle (global)
+};
+
+struct NextState {
+    void* x;
+    void* v;
+    double* T;
+    double* rho;
+};
+
+struct WallState {
+    void* x;       // VecT
+    void* nrm;     // VecT
+    void* v;       // VecT
+    double* gap;
+    double* T;
+    double* kappa;
+    int32_t* kind;
+    int32_t* start;  // global cells + 1
+    float4* fa;      // FP32: 2D (xr, yr, nx, ny)    3D (xr, yr, zr, gap)
+    float4* fb;      // FP32: 2D (vx, vy, gap, T)    3D (nx, ny, nz, T)
+    float4* fc;      // FP32: 2D (kappa, kind, -, -) 3D (vx, vy, vz, kappa)
+    int32_t* cell;
+    int64_t n;
+};
+
+struct SortScratch {
+    int32_t* key;    // per particle (unsorted index): global cell key or kDeadKey
+    int32_t* slot;   // per particle: arrival slot inside its cell
+    int32_t* count;  // per cell
+    int32_t* start;  // per cell + 1: exclusive scan of count
+    int32_t* tmp;    // per sorted position: id by arrival slot
+    int32_t* block_sums;
+    int32_t* n_live;    // device scalar: live particles after the last sort
+    int32_t* status;    // device scalar: status bits
+    int64_t* scene_step;  // per scene: number of the step being run
+};
+
+// ---------------------------------------------------------------- grid
+__device__ __forceinline__ int32_t cell_coord(double x, const SceneDev& S, int a) {
+    const double u = (x - S.lo[a]) * S.inv_cell[a];
+    if (!(u >= 0.0)) return 0;
+    const double f = floor(u);
+    if (f >= (double)(S.n[a] - 1)) return S.n[a] - 1;
+    return (int32_t)f;
+}
+
+// Whether coordinate lies outside the grid (the particle was clamped into an edge cell).
+__device__ __forceinline__ bool outside_grid(double x, const SceneDev& S, int a) {
+    const double u = (x - S.lo[a]) * S.inv_cell[a];
+    return !(u >= 0.0) || u >= (double)S.n[a];
+}
+
+// ---------------------------------------------------------------- Julia numerics
+// Base ^(x::Float64, n::Integer) (compensated power by squaring; exact products by fma).
+__device__ __forceinline__ double jl_powi(double x, int n) {
+    if (n == 0) return 1.0;
+    if (n == 3) return __dmul_rn(__dmul_rn(x, x), x);
+    double y = 1.0, xnlo = 0.0, ynlo = 0.0;
+    if (n < 0) {
+        const double rx = 1.0 / x;
+        if (n == -2) return __dmul_rn(rx, rx);
+        if (isfinite(x)) xnlo = __dmul_rn(-fma(x, rx, -1.0), rx);
+        x = rx;
+        n = -n;
+    }
+    while (n > 1) {
+        if (n & 1) {
+            const double err = fma(y, xnlo, __dmul_rn(x, ynlo));
+            const double yh = __dmul_rn(x, y);
+            const double yl = fma(x, y, -yh);
+            y = yh;
+            ynlo = __dadd_rn(yl, err);
+        }
+        const double err = __dmul_rn(__dmul_rn(x, 2.0), xnlo);
+        const double xh = __dmul_rn(x, x);
+        const double xl = fma(x, x, -xh);
+        x = xh;
+        xnlo = __dadd_rn(xl, err);
+        n >>= 1;
+    }
+    const double err = fma(y, xnlo, __dmul_rn(x, ynlo));
+    return (isfinite(x) && isfinite(err)) ? fma(x, y, err) : __dmul_rn(x, y);
+}
+
+}  // namespace sph

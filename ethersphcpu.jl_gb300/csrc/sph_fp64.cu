@@ -1,0 +1,362 @@
+// sph_fp64.cu — plain FP64 gather kernels of the WCSPH step (compiled -fmad=false).
+//
+// K4 continuity + updateDensity! + updatePressure!   (Continuity.jl:8-17,
+//    UpdateDensity.jl:8-12, UpdatePressure.jl:8-16)
+// K5 momentum (pressure, viscosity, compulsive wall, heat) + updateTemperature! +
+//    updateVelocity! + updatePosition!, fused with the out-of-domain check and the
+//    cell hash of the next step's sort   (PressureForce.jl, ViscosityForce.jl,
+//    WallForce.jl, ThermalConduction.jl, SelfAction/*.jl, FluidWallSolve.jl:37-81)
+// K6 Shepard density re-initialisation  (ReconstructValue.jl:22-57)
+//
+// One thread per fluid particle in sorted (cell, id) order; each thread sums its own
+// full neighbour list in a fixed order (cells z, y, x; particles by id), so there are
+// no atomics on the physics and results are deterministic.  Walls are visited after
+// fluid neighbours.  The reference scatters each unordered pair to both particles
+// with atomics; every pair term here is the bitwise same number the reference adds
+// (the pair formulas are antisymmetric under exact negation), only the order of the
+// additions differs.
+#include "sph_physics.cuh"
+#include "sph_kernels.h"
+
+namespace sph {
+
+// Solve variants: which wall terms and which body force.
+enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2 };
+
+template <int DIM, int KK>
+__global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restrict__ scenes, SortedState st,
+                                                         const int32_t* __restrict__ start,
+                                                         const int32_t* __restrict__ n_live, int32_t cap) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *n_live) return;
+    const SceneDev& S = scenes[st.scene[i]];
+    const V* __restrict__ x = (const V*)st.x;
+    const V* __restrict__ v = (const V*)st.v;
+    const V xi = x[i];
+    const V vi = v[i];
+    int32_t c[3];
+    cell_of<DIM>(xi, S, c);
+    double drho = 0.0;
+    walk_cells<DIM>(S, start, c, [&](int jb, int je) {
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            const V xj = x[j];
+            double rv[DIM];
+            make_rvec<DIM>(xi, xj, S, rv);
+            const double d2 = norm_sq<DIM>(rv);
+            if (!(d2 <= S.rc2)) continue;
+            const double r = sqrt(d2);
+            double W, dW;
+            kernel_wdw<KK>(r, S, W, dW);
+            double g[DIM];
+            grad_vec<DIM>(dW, r, rv, g);
+            const V vj = v[j];
+            double vv[DIM];
+            vv[0] = vi.x - vj.x;
+            vv[1] = vi.y - vj.y;
+            if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vj, DIM - 1);
+            drho += dotd<DIM>(vv, g) * st.m[j];
+        }
+    });
+    double rho = st.rho[i];
+    rho += drho * S.dt;  // written to rhoc, so the kernel can be re-run on the same input
+    const double rr = rho / S.rho0;
+    const double p = S.b * (jl_powi(rr, S.gamma) - 1.0) + S.p0;
+    const double cs = S.c0 * sqrt(jl_powi(rr, S.gamma - 1));
+    st.rhoc[i] = rho;
+    st.p[i] = p;
+    st.c[i] = cs;
+    st.P[i] = p / (rho * rho);
+}
+
+template <int DIM, int KK, int MODE>
+__global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restrict__ scenes, SortedState st,
+                                                       NextState nx, WallState wl, SortScratch sc,
+                                                       int32_t cap) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    const int64_t step = sc.scene_step[s];
+    const V* __restrict__ x = (const V*)st.x;
+    const V* __restrict__ v = (const V*)st.v;
+    const V xi = x[i];
+    const V vi = v[i];
+    const double rho_i = st.rhoc[i];
+    const double P_i = st.P[i];
+    const double m_i = st.m[i];
+    const double gap_i = st.gap[i];
+    const double c_i = st.c[i];
+    const double mu_i = S.nu0 * rho_i;
+    double T_i = 0.0, kap_i = 0.0, cp_i = 1.0;
+    if (MODE == kModeThermal) {
+        T_i = st.T[i];
+        kap_i = st.kappa[i];
+        cp_i = st.cp[i];
+    }
+    // W((gap_i + gap_j)/2) of the tensile term; with uniform gaps it is W(gap_i).
+    const double Wg_i = kernel_w<KK>(gap_i, S);
+    int32_t c[3];
+    cell_of<DIM>(xi, S, c);
+    double dv[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) dv[k] = 0.0;
+    double dT = 0.0;
+
+    // ---- fluid neighbours: pressureForce! + viscosityForce! (+ thermalConduction!)
+    walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            const V xj = x[j];
+            double rv[DIM];
+            make_rvec<DIM>(xi, xj, S, rv);
+            const double d2 = norm_sq<DIM>(rv);
+            if (!(d2 <= S.rc2)) continue;
+            const double r = sqrt(d2);
+            double W, dW;
+            kernel_wdw<KK>(r, S, W, dW);
+            double g[DIM];
+            grad_vec<DIM>(dW, r, rv, g);
+            const V vj = v[j];
+            double vv[DIM];
+            vv[0] = vi.x - vj.x;
+            vv[1] = vi.y - vj.y;
+            if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vj, DIM - 1);
+            const double rho_j = st.rhoc[j];
+            const double m_j = st.m[j];
+            // PressureForce.jl:14-19
+            double prho2 = P_i + st.P[j];
+            const double Wg = S.uniform_gap ? Wg_i : kernel_w<KK>((gap_i + st.gap[j]) / 2.0, S);
+            prho2 += fabs(prho2) * 0.01 * W / Wg;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) dv[k] += -m_j * prho2 * g[k];
+            // ViscosityForce.jl:15-23
+            const double sum_rho = rho_i + rho_j;
+            const double mu_j = S.nu0 * rho_j;
+            const double f = 4.0 * (mu_i + mu_j) * r * dW / (sum_rho * sum_rho) / (r * r + S.hh001);
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) dv[k] += m_j * f * vv[k];
+            if (MODE == kModeThermal) {  // ThermalConduction.jl:15-21
+                const double kap_j = st.kappa[j];
+                const double keq = 2.0 * kap_i * kap_j / (kap_i + kap_j);
+                const double dq = 2.0 * keq * r * dW / rho_i / rho_j / (r * r + S.hh001) * (T_i - st.T[j]);
+                dT += dq * m_j / cp_i;
+            }
+        }
+    });
+
+    // ---- walls: wallForce! (+ background pressureForce!) + viscosityForce! (+ heat)
+    if (wl.n > 0) {
+        const V* __restrict__ wx = (const V*)wl.x;
+        const V* __restrict__ wn = (const V*)wl.nrm;
+        const V* __restrict__ wv = (const V*)wl.v;
+        const double Wgap_bg = Wg_i;  // kernelValue(p_i.gap_) of PressureForce.jl:30
+        walk_cells<DIM>(S, wl.start, c, [&](int jb, int je) {
+            for (int w = jb; w < je; ++w) {
+                const V xw = wx[w];
+                double rv[DIM];
+                make_rvec<DIM>(xi, xw, S, rv);
+                const double d2 = norm_sq<DIM>(rv);
+                if (!(d2 <= S.rc2)) continue;
+                const double r = sqrt(d2);
+                double W, dW;
+                kernel_wdw<KK>(r, S, W, dW);
+                double g[DIM];
+                grad_vec<DIM>(dW, r, rv, g);
+                const V vw = wv[w];
+                const V nw = wn[w];
+                double vv[DIM], n[DIM];
+                vv[0] = vi.x - vw.x;
+                vv[1] = vi.y - vw.y;
+                n[0] = nw.x;
+                n[1] = nw.y;
+                if (DIM == 3) {
+                    vv[DIM - 1] = comp(vi, DIM - 1) - comp(vw, DIM - 1);
+                    n[DIM - 1] = comp(nw, DIM - 1);
+                }
+                const double gw = wl.gap[w];
+                // WallForce.jl:15-28 (Rogers & Dalrymple 2008)
+                {
+                    const double psi = fabs(dotd<DIM>(rv, n));
+                    double t = r * r - psi * psi;
+                    t = isnan(t) ? t : (t > 0.0 ? t : 0.0);
+                    const double xi_ = sqrt(t);
+                    const double q = psi / gw;
+                    if (!(q > 1.0 || xi_ > gw)) {
+                        const double pxi = fabs((1.0 + cos(CUDART_PI * xi_ / gw)) / 2.0);
+                        const double vert = dotd<DIM>(vv, n);
+                        const double beta = vert > 0.0 ? 0.0 : 1.0;
+                        const double rpsi =
+                            (0.01 * (c_i * c_i) + beta * c_i * fabs(vert)) / S.h * fabs(1.0 - q) / sqrt(q);
+                        const double wf = rpsi * pxi;
+#pragma unroll
+                        for (int k = 0; k < DIM; ++k) dv[k] += wf * n[k];
+                    }
+                }
+                if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
+                    double prho2 = P_i + S.P_bg;
+                    prho2 += fabs(prho2) * 0.01 * W / Wgap_bg;
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) dv[k] += -m_i * prho2 * g[k];
+                }
+                {  // ViscosityForce.jl:34-44
+                    const double sum_rho = 2.0 * rho_i;
+                    const double f = 8.0 * mu_i * r * dW / (sum_rho * sum_rho) / (r * r + S.hh001);
+                    const double vert = dotd<DIM>(vv, n);
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) dv[k] += m_i * f * (vv[k] - vert * n[k]);
+                }
+                if (MODE == kModeThermal && wl.kind[w] == SPH_WALL_THERMOSTATIC) {  // ThermalConduction.jl:31-35
+                    const double dq = S.inv_cp_d * (kap_i + wl.kappa[w]) * r * dW / rho_i / S.rho0 /
+                                      (r * r + S.hh001) * (T_i - wl.T[w]);
+                    dT += dq * m_i;
+                }
+            }
+        });
+    }
+
+    // ---- updateTemperature!, updateVelocity!, updatePosition!
+    const double dt = S.dt;
+    double body[DIM];
+    if (MODE == kModeThermal) {
+        T_i += dt * dT;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) body[k] = S.bous[k] * (T_i - S.t0);
+        nx.T[i] = T_i;
+    } else {
+        if (nx.T) nx.T[i] = st.T[i];  // thermal particles in a solve without heat terms
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) body[k] = S.g[k];
+    }
+    double vn[DIM], xn[DIM];
+    vn[0] = vi.x;
+    vn[1] = vi.y;
+    xn[0] = xi.x;
+    xn[1] = xi.y;
+    if (DIM == 3) {
+        vn[DIM - 1] = comp(vi, DIM - 1);
+        xn[DIM - 1] = comp(xi, DIM - 1);
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vn[k] += body[k] * dt;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) vn[k] += dv[k] * dt;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) xn[k] += vn[k] * dt - dv[k] * S.dtdt / 2.0;
+    if (S.periodic_x) {
+        if (xn[0] >= S.wrap_hi) xn[0] -= S.period;
+        else if (xn[0] < S.lo[0]) xn[0] += S.period;
+    }
+    V xo, vo;
+    xo.x = xn[0];
+    xo.y = xn[1];
+    vo.x = vn[0];
+    vo.y = vn[1];
+    if constexpr (DIM == 3) {
+        xo.z = xn[2];
+        xo.w = 0.0;
+        vo.z = vn[2];
+        vo.w = 0.0;
+    }
+    ((V*)nx.x)[i] = xo;
+    ((V*)nx.v)[i] = vo;
+    nx.rho[i] = rho_i;
+
+    // ---- non-finite state, out-of-domain check, next step's cell hash
+    bool finite = isfinite(rho_i);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) finite &= isfinite(xn[k]) & isfinite(vn[k]);
+    if (!finite && S.nan_check) atomicOr(sc.status, kStatusNonFinite);
+    bool dead = false;
+    if (S.check_enabled && is_step(step, S.check_interval)) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) dead |= (xn[k] > S.check_hi[k]) | (xn[k] < S.check_lo[k]);
+    }
+    if (dead) {
+        sc.key[i] = kDeadKey;
+    } else {
+        const int32_t key = cell_key<DIM>(xo, S);
+        sc.key[i] = key;
+        sc.slot[i] = atomicAdd(sc.count + key, 1);
+    }
+}
+
+template <int DIM, int KK>
+__global__ void __launch_bounds__(128) k_reinit_fp64(const SceneDev* __restrict__ scenes, SortedState st,
+                                                     NextState nx, SortScratch sc, int32_t cap, int force) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    if (!force && !is_step(sc.scene_step[s], S.reinit_interval)) return;
+    const V* __restrict__ x = (const V*)st.x;
+    const V xi = x[i];
+    int32_t c[3];
+    cell_of<DIM>(xi, S, c);
+    double sw = 0.0, sws = 0.0;
+    walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            double rv[DIM];
+            make_rvec<DIM>(xi, x[j], S, rv);
+            const double d2 = norm_sq<DIM>(rv);
+            if (!(d2 <= S.rc2)) continue;
+            const double W = kernel_w<KK>(sqrt(d2), S);
+            const double m_j = st.m[j], rho_j = st.rhoc[j];
+            sw += W * m_j / rho_j;
+            sws += W * m_j / rho_j * rho_j;
+        }
+    });
+    const double m_i = st.m[i], rho_i = st.rhoc[i];
+    sw += S.k0 * m_i / rho_i;
+    sws += S.k0 * m_i / rho_i * rho_i;
+    nx.rho[i] = sws / sw;
+}
+
+// ---------------------------------------------------------------- launchers
+namespace {
+template <int DIM, int KK>
+void launch_k4(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_continuity_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+}
+template <int DIM, int KK, int MODE>
+void launch_k5(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_momentum_fp64<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap);
+}
+template <int DIM, int KK>
+void launch_k6(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_reinit_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap, L.force_reinit);
+}
+
+template <int DIM>
+void dispatch_kk(int kk, int stage, int mode, const LaunchCtx& L) {
+#define SPH_KK_CASE(KKV)                                                        \
+    case KKV:                                                                   \
+        if (stage == 0) launch_k4<DIM, KKV>(L);                                 \
+        else if (stage == 2) launch_k6<DIM, KKV>(L);                            \
+        else if (mode == kModeFluidWall) launch_k5<DIM, KKV, kModeFluidWall>(L); \
+        else if (mode == kModeWallPressure) launch_k5<DIM, KKV, kModeWallPressure>(L); \
+        else launch_k5<DIM, KKV, kModeThermal>(L);                              \
+        break;
+    switch (kk) {
+        SPH_KK_CASE(SPH_KERNEL_CUBIC_SPLINE)
+        SPH_KK_CASE(SPH_KERNEL_GAUSSIAN)
+        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C2)
+        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C4)
+    }
+#undef SPH_KK_CASE
+}
+}  // namespace
+
+void launch_physics_fp64(int stage, const LaunchCtx& L) {
+    if (L.dim == 2) dispatch_kk<2>(L.kernel, stage, L.mode, L);
+    else dispatch_kk<3>(L.kernel, stage, L.mode, L);
+}
+
+}  // namespace sph

@@ -1,0 +1,48 @@
+// sph_kernels.h — host-side launch interface of the device kernels (internal).
+#pragma once
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+// Everything one stage launch needs.  Filled by the engine for the current buffer
+// parity; plain values, so a captured CUDA graph bakes them in.
+struct LaunchCtx {
+    cudaStream_t stream;
+    int dim;
+    int kernel;   // SPH_KERNEL_*
+    int mode;     // 0 fluid-wall, 1 wall pressure, 2 thermal
+    int thermal;
+    int precision;
+    int32_t cap;          // particle capacity (grid size of per-particle kernels)
+    int32_t total_cells;  // cells over all scenes
+    int32_t nscenes;
+    const SceneDev* scenes;
+    SortedState st;   // current sorted state
+    SortedState st2;  // the other sorted buffer (output of the sort)
+    NextState nx;
+    WallState wl;
+    SortScratch sc;
+    int32_t* n_next;  // live count after the sort being built
+    int force_reinit; // 1: re-initialise every scene regardless of its step (stage timing)
+};
+
+// stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init
+void launch_physics_fp64(int stage, const LaunchCtx& L);
+void launch_physics_fp32(int stage, const LaunchCtx& L);
+
+// Cell hash of the unsorted positions in L.nx.x (used once after an upload).
+void launch_hash(const LaunchCtx& L);
+// Exclusive scan of sc.count into sc.start; writes the live total to *L.n_next.
+// When advance != 0 it also increments every scene's step counter.
+void launch_scan(const LaunchCtx& L, int advance);
+// Stable (cell, id) placement: tmp fill, then rank + copy of every field into L.st2.
+void launch_place(const LaunchCtx& L);
+// FP64 reductions: out[0] = sum m, out[1] = sum m|v|^2/2, out[2] = max |v|.
+void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out);
+// Unique fluid pairs (sorted j > i) and fluid-wall pairs within r_cut.
+void launch_count_pairs(const LaunchCtx& L, unsigned long long* d_counts);
+
+int scan_max_cells();
+
+}  // namespace sph

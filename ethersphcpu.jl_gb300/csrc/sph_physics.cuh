@@ -1,0 +1,212 @@
+// sph_physics.cuh — FP64 pair physics of the WCSPH step, in the reference's IEEE
+// operation order.  Compiled with -fmad=false so that no a*b+c is contracted; with
+// the sequential per-particle neighbour order this makes a step reproducible bit for
+// bit across runs and comparable bit for bit with a CPU restatement (up to the last
+// ulp of cos/exp, the only library functions on the path).
+#pragma once
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------- SPHKernel
+// W(r) and dW/dr.  CubicSpline.jl:39-73, Gaussian.jl:31-56, WendlandC2.jl:38-63,
+// WendlandC4.jl:38-54.  q = r/h is formed once (the reference forms the same value
+// twice).  kw_a / kg_a are the leading constant products of each formula, formed on
+// the host in the same order.
+template <int KK>
+__device__ __forceinline__ void kernel_wdw(double r, const SceneDev& S, double& W, double& dW) {
+    const double q = r / S.h;
+    if (KK == SPH_KERNEL_CUBIC_SPLINE) {
+        if (q < 1.0) {
+            W = S.kw_a * (3.0 * (q * q) * (q - 2.0) + 4.0);
+            dW = S.kg_a * q * (3.0 * q - 4.0);
+        } else if (q < 2.0) {
+            const double t = 2.0 - q;
+            W = S.kw_a * (t * t * t);
+            dW = -S.kg_a * (t * t);
+        } else {
+            W = 0.0;
+            dW = 0.0;
+        }
+    } else if (KK == SPH_KERNEL_GAUSSIAN) {
+        if (q < 3.0) {
+            const double e = exp(-(q * q));
+            W = S.kw_a * e;
+            dW = S.kg_a * q * e;
+        } else {
+            W = 0.0;
+            dW = 0.0;
+        }
+    } else if (KK == SPH_KERNEL_WENDLAND_C2) {
+        if (q < 2.0) {
+            const double t = 2.0 - q;
+            W = S.kw_a * jl_powi(t, 4) * (1.0 + 2.0 * q) * 0.0625;  // /16 is exact as *2^-4
+            dW = S.kg_a * q * (t * t * t);
+        } else {
+            W = 0.0;
+            dW = 0.0;
+        }
+    } else {  // WendlandC4
+        if (q < 2.0) {
+            const double t = 2.0 - q;
+            W = S.kw_a * jl_powi(t, 6) * (35.0 * (q * q) + 36.0 * q + 12.0) / 768.0;
+            dW = S.kg_a * (35.0 / 96.0 * (q * q) + 7.0 / 48.0 * q) * jl_powi(t, 5);
+        } else {
+            W = 0.0;
+            dW = 0.0;
+        }
+    }
+}
+
+template <int KK>
+__device__ __forceinline__ double kernel_w(double r, const SceneDev& S) {
+    const double q = r / S.h;
+    if (KK == SPH_KERNEL_CUBIC_SPLINE) {
+        if (q < 1.0) return S.kw_a * (3.0 * (q * q) * (q - 2.0) + 4.0);
+        if (q < 2.0) {
+            const double t = 2.0 - q;
+            return S.kw_a * (t * t * t);
+        }
+        return 0.0;
+    } else if (KK == SPH_KERNEL_GAUSSIAN) {
+        if (q < 3.0) return S.kw_a * exp(-(q * q));
+        return 0.0;
+    } else if (KK == SPH_KERNEL_WENDLAND_C2) {
+        if (q < 2.0) return S.kw_a * jl_powi(2.0 - q, 4) * (1.0 + 2.0 * q) * 0.0625;
+        return 0.0;
+    } else {
+        if (q < 2.0) return S.kw_a * jl_powi(2.0 - q, 6) * (35.0 * (q * q) + 36.0 * q + 12.0) / 768.0;
+        return 0.0;
+    }
+}
+
+// ---------------------------------------------------------------- pair geometry
+template <int DIM>
+struct Pair {
+    double rv[DIM];
+    double d2;
+};
+
+template <int DIM, typename V>
+__device__ __forceinline__ void make_rvec(const V& xi, const V& xj, const SceneDev& S, double rv[DIM]) {
+    rv[0] = xi.x - xj.x;
+    rv[1] = xi.y - xj.y;
+    if (DIM == 3) rv[DIM - 1] = comp(xi, DIM - 1) - comp(xj, DIM - 1);
+    if (S.periodic_x) {
+        if (rv[0] > S.half_period) rv[0] -= S.period;
+        else if (rv[0] < -S.half_period) rv[0] += S.period;
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ double norm_sq(const double rv[DIM]) {
+    double s = rv[0] * rv[0] + rv[1] * rv[1];
+    if (DIM == 3) s += rv[DIM - 1] * rv[DIM - 1];
+    return s;
+}
+
+// grad W = dW * normalize(r_vec), NaN components -> 0 (Neighbour.jl:76-84).
+// normalize: LinearAlgebra generic_norm2 + __normalize!; for ordinary magnitudes
+// the norm is sqrt(d2) = r bit for bit.
+template <int DIM>
+__device__ __forceinline__ void grad_vec(double dW, double r, const double rv[DIM], double g[DIM]) {
+    double maxabs = fabs(rv[0]);
+    bool nan_in = isnan(rv[0]);
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) {
+        const double a = fabs(rv[k]);
+        nan_in |= isnan(a);
+        maxabs = a > maxabs ? a : maxabs;
+    }
+    double nrm;
+    if (nan_in) {
+        nrm = CUDART_NAN;
+    } else if (maxabs == 0.0 || isinf(maxabs)) {
+        nrm = maxabs;
+    } else if (isfinite((double)DIM * maxabs * maxabs) && maxabs * maxabs != 0.0) {
+        nrm = r;
+    } else {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            const double t = rv[k] / maxabs;
+            s += t * t;
+        }
+        nrm = maxabs * sqrt(s);
+    }
+    const double delta = 1.0 / 1.7976931348623157e308;
+    double a[DIM];
+    if (nrm >= delta) {
+        const double inv = 1.0 / nrm;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] = rv[k] * inv;
+    } else {
+        const double ed = 2.220446049250313e-16 / delta;
+        const double inv = 1.0 / (nrm * ed);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] = (rv[k] * ed) * inv;
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        const double gk = dW * a[k];
+        g[k] = isnan(gk) ? 0.0 : gk;
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ double dotd(const double a[DIM], const double b[DIM]) {
+    double s = a[0] * b[0] + a[1] * b[1];
+    if (DIM == 3) s += a[DIM - 1] * b[DIM - 1];
+    return s;
+}
+
+// ---------------------------------------------------------------- neighbour walk
+// Visits the neighbour cells of cell c in (z, y, x) order, each x-run of up to three
+// cells as one contiguous range of the sorted arrays (cells of a row are adjacent in
+// key space).  A periodic x axis visits its three cells one by one (wrapping).
+template <int DIM, typename F>
+__device__ __forceinline__ void walk_cells(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
+                                           F&& f) {
+    const int zr = DIM == 3 ? 1 : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const int z = c[2] + dz;
+        if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = c[1] + dy;
+            if (y < 0 || y >= S.n[1]) continue;
+            const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
+            if (!S.periodic_x) {
+                const int x0 = c[0] > 0 ? c[0] - 1 : 0;
+                const int x1 = c[0] + 1 < S.n[0] ? c[0] + 1 : S.n[0] - 1;
+                f(__ldg(start + row + x0), __ldg(start + row + x1 + 1));
+            } else {
+                for (int dx = -1; dx <= 1; ++dx) {
+                    int x = c[0] + dx;
+                    x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
+                    f(__ldg(start + row + x), __ldg(start + row + x + 1));
+                }
+            }
+        }
+    }
+}
+
+template <int DIM, typename V>
+__device__ __forceinline__ void cell_of(const V& x, const SceneDev& S, int32_t c[3]) {
+    c[0] = cell_coord(x.x, S, 0);
+    c[1] = cell_coord(x.y, S, 1);
+    c[2] = DIM == 3 ? cell_coord(comp(x, DIM - 1), S, 2) : 0;
+}
+
+template <int DIM, typename V>
+__device__ __forceinline__ int32_t cell_key(const V& x, const SceneDev& S) {
+    int32_t c[3];
+    cell_of<DIM>(x, S, c);
+    return S.cell_off + (c[2] * S.n[1] + c[1]) * S.n[0] + c[0];
+}
+
+__device__ __forceinline__ bool is_step(int64_t step, int64_t interval) {
+    return interval > 0 && step % interval == 0;
+}
+
+}  // namespace sph

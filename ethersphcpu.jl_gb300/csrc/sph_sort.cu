@@ -1,0 +1,318 @@
+// sph_sort.cu — the per-step cell list: hash, exclusive scan, stable (cell, id)
+// placement with the SoA reorder, plus FP64 reductions and the pair counter.
+//
+// Replaces CellListMap.update!/neighborlist! + findNeighbours! (Neighbour.jl:88-128,
+// FluidWallSolve.jl:21-35): instead of a materialised pair list, particles are kept
+// physically sorted by (cell key, id) and every gather kernel walks the 9 (2D) or 27
+// (3D) neighbour cells.  Counting sort:
+//   1. hash: key = cell of the position, slot = atomicAdd(count[key]) (fused into the
+//      momentum kernel for every step after the first)
+//   2. exclusive scan of count -> start (3 kernels: tile sums, top scan, tile scan)
+//   3. fill: tmp[start[key] + slot] = id       (arrival order, nondeterministic)
+//   4. place: rank = #ids in the cell smaller than mine -> destination start[key]+rank,
+//      copy every field there (deterministic: the order is (cell, id) whatever the
+//      arrival order was)
+#include "sph_physics.cuh"
+#include "sph_kernels.h"
+
+namespace sph {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;  // cells per tile
+constexpr int kScanTopThreads = 1024;
+constexpr int kScanTopItems = 16;
+
+int scan_max_cells() { return kScanTile * kScanTopThreads * kScanTopItems; }
+
+// ---------------------------------------------------------------- hash (after upload)
+template <int DIM>
+__global__ void k_hash(const SceneDev* __restrict__ scenes, NextState nx, SortedState st, SortScratch sc,
+                       int32_t cap) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const SceneDev& S = scenes[st.scene[i]];
+    const V x = ((const V*)nx.x)[i];
+    const int32_t key = cell_key<DIM>(x, S);
+    sc.key[i] = key;
+    sc.slot[i] = atomicAdd(sc.count + key, 1);
+}
+
+// ---------------------------------------------------------------- scan
+// Block-wide exclusive scan of one value per thread; returns the prefix, *total gets
+// the block sum.
+template <int THREADS>
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t v, int32_t* warp_sums, int32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int NW = THREADS / 32;
+        int32_t w = lane < NW ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < NW) warp_sums[lane] = w;  // inclusive
+    }
+    __syncthreads();
+    const int32_t warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[THREADS / 32 - 1];
+    return warp_prefix + inc - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ count, int32_t n,
+                                                            int32_t* __restrict__ tile_sums) {
+    __shared__ int32_t red[kScanThreads / 32];
+    const int base = blockIdx.x * kScanTile;
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = base + k * kScanThreads + threadIdx.x;
+        s += idx < n ? count[idx] : 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += red[w];
+        tile_sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kScanTopThreads) k_scan_top(int32_t* __restrict__ tile_sums, int32_t ntiles,
+                                                             int32_t* __restrict__ start_total,
+                                                             int32_t* __restrict__ n_next,
+                                                             int64_t* __restrict__ scene_step, int32_t nscenes,
+                                                             int advance) {
+    __shared__ int32_t warp_sums[kScanTopThreads / 32];
+    int32_t v[kScanTopItems];
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanTopItems; ++k) {
+        const int idx = threadIdx.x * kScanTopItems + k;
+        v[k] = idx < ntiles ? tile_sums[idx] : 0;
+        local += v[k];
+    }
+    int32_t total;
+    int32_t run = block_exclusive_scan<kScanTopThreads>(local, warp_sums, &total);
+#pragma unroll
+    for (int k = 0; k < kScanTopItems; ++k) {
+        const int idx = threadIdx.x * kScanTopItems + k;
+        if (idx < ntiles) tile_sums[idx] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) {
+        *start_total = total;
+        *n_next = total;
+    }
+    if (advance)
+        for (int s = threadIdx.x; s < nscenes; s += blockDim.x) scene_step[s] += 1;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __restrict__ count, int32_t n,
+                                                           const int32_t* __restrict__ tile_offsets,
+                                                           int32_t* __restrict__ start) {
+    __shared__ int32_t tile[kScanTile];
+    __shared__ int32_t warp_sums[kScanThreads / 32];
+    const int base = blockIdx.x * kScanTile;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = k * kScanThreads + threadIdx.x;
+        tile[idx] = base + idx < n ? count[base + idx] : 0;
+    }
+    __syncthreads();
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) local += tile[threadIdx.x * kScanItems + k];
+    int32_t total;
+    int32_t run = block_exclusive_scan<kScanThreads>(local, warp_sums, &total) + tile_offsets[blockIdx.x];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = threadIdx.x * kScanItems + k;
+        const int32_t c = tile[idx];
+        tile[idx] = run;
+        run += c;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = k * kScanThreads + threadIdx.x;
+        if (base + idx < n) start[base + idx] = tile[idx];
+    }
+}
+
+// ---------------------------------------------------------------- placement
+__global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t key = sc.key[i];
+    if (key == kDeadKey) return;
+    sc.tmp[sc.start[key] + sc.slot[i]] = id[i];
+}
+
+template <int DIM, bool THERMAL>
+__global__ void k_place(SortedState src, NextState nx, SortedState dst, SortScratch sc, int32_t cap) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t key = sc.key[i];
+    if (key == kDeadKey) return;
+    const int32_t b = sc.start[key], e = sc.start[key + 1];
+    const int32_t myid = src.id[i];
+    int32_t rank = 0;
+    for (int32_t t = b; t < e; ++t) rank += sc.tmp[t] < myid;
+    const int32_t d = b + rank;
+    ((V*)dst.x)[d] = ((const V*)nx.x)[i];
+    ((V*)dst.v)[d] = ((const V*)nx.v)[i];
+    dst.rho[d] = nx.rho[i];
+    dst.p[d] = src.p[i];
+    dst.c[d] = src.c[i];
+    dst.m[d] = src.m[i];
+    dst.gap[d] = src.gap[i];
+    dst.id[d] = myid;
+    dst.scene[d] = src.scene[i];
+    if (THERMAL) {
+        dst.T[d] = nx.T[i];
+        dst.kappa[d] = src.kappa[i];
+        dst.cp[d] = src.cp[i];
+    }
+}
+
+// ---------------------------------------------------------------- reductions
+constexpr int kStatThreads = 256;
+constexpr int kStatBlocks = 152;
+
+template <int DIM>
+__global__ void __launch_bounds__(kStatThreads) k_stats_partial(SortedState st, const int32_t* __restrict__ n_live,
+                                                               double* __restrict__ partials) {
+    using V = typename VecT<DIM>::T;
+    __shared__ double sm[3][kStatThreads];
+    const int n = *n_live;
+    double m = 0.0, ke = 0.0, vmax = 0.0;
+    for (int i = blockIdx.x * kStatThreads + threadIdx.x; i < n; i += gridDim.x * kStatThreads) {
+        const V v = ((const V*)st.v)[i];
+        double v2 = v.x * v.x + v.y * v.y;
+        if (DIM == 3) v2 += comp(v, DIM - 1) * comp(v, DIM - 1);
+        m += st.m[i];
+        ke += 0.5 * st.m[i] * v2;
+        vmax = fmax(vmax, sqrt(v2));
+    }
+    sm[0][threadIdx.x] = m;
+    sm[1][threadIdx.x] = ke;
+    sm[2][threadIdx.x] = vmax;
+    __syncthreads();
+    for (int s = kStatThreads / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sm[0][threadIdx.x] += sm[0][threadIdx.x + s];
+            sm[1][threadIdx.x] += sm[1][threadIdx.x + s];
+            sm[2][threadIdx.x] = fmax(sm[2][threadIdx.x], sm[2][threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[3 * blockIdx.x + 0] = sm[0][0];
+        partials[3 * blockIdx.x + 1] = sm[1][0];
+        partials[3 * blockIdx.x + 2] = sm[2][0];
+    }
+}
+
+__global__ void k_stats_final(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double m = 0.0, ke = 0.0, vmax = 0.0;
+    for (int b = 0; b < nblocks; ++b) {
+        m += partials[3 * b];
+        ke += partials[3 * b + 1];
+        vmax = fmax(vmax, partials[3 * b + 2]);
+    }
+    out[0] = m;
+    out[1] = ke;
+    out[2] = vmax;
+}
+
+template <int DIM>
+__global__ void k_count_pairs(const SceneDev* __restrict__ scenes, SortedState st, WallState wl, SortScratch sc,
+                              int32_t cap, unsigned long long* counts) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const SceneDev& S = scenes[st.scene[i]];
+    const V* x = (const V*)st.x;
+    const V xi = x[i];
+    int32_t c[3];
+    cell_of<DIM>(xi, S, c);
+    unsigned long long a = 0, b = 0;
+    walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
+        for (int j = jb; j < je; ++j) {
+            if (j <= i) continue;
+            double rv[DIM];
+            make_rvec<DIM>(xi, x[j], S, rv);
+            a += norm_sq<DIM>(rv) <= S.rc2;
+        }
+    });
+    if (wl.n > 0) {
+        const V* wx = (const V*)wl.x;
+        walk_cells<DIM>(S, wl.start, c, [&](int jb, int je) {
+            for (int w = jb; w < je; ++w) {
+                double rv[DIM];
+                make_rvec<DIM>(xi, wx[w], S, rv);
+                b += norm_sq<DIM>(rv) <= S.rc2;
+            }
+        });
+    }
+    atomicAdd(counts, a);
+    atomicAdd(counts + 1, b);
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_hash(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    if (L.dim == 2) k_hash<2><<<grid, 128, 0, L.stream>>>(L.scenes, L.nx, L.st, L.sc, L.cap);
+    else k_hash<3><<<grid, 128, 0, L.stream>>>(L.scenes, L.nx, L.st, L.sc, L.cap);
+}
+
+void launch_scan(const LaunchCtx& L, int advance) {
+    const int n = L.total_cells;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
+    k_scan_top<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
+                                                    L.sc.scene_step, L.nscenes, advance);
+    k_scan_down<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, L.sc.start);
+}
+
+void launch_place(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_fill<<<grid, 128, 0, L.stream>>>(L.sc, L.st.id, L.cap);
+    if (L.dim == 2) {
+        if (L.thermal) k_place<2, true><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+        else k_place<2, false><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+    } else {
+        if (L.thermal) k_place<3, true><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+        else k_place<3, false><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+    }
+}
+
+void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out) {
+    if (L.dim == 2) k_stats_partial<2><<<kStatBlocks, kStatThreads, 0, L.stream>>>(L.st, L.sc.n_live, d_partials);
+    else k_stats_partial<3><<<kStatBlocks, kStatThreads, 0, L.stream>>>(L.st, L.sc.n_live, d_partials);
+    k_stats_final<<<1, 32, 0, L.stream>>>(d_partials, kStatBlocks, d_out);
+}
+
+void launch_count_pairs(const LaunchCtx& L, unsigned long long* d_counts) {
+    const int grid = (L.cap + 127) / 128;
+    if (L.dim == 2) k_count_pairs<2><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.wl, L.sc, L.cap, d_counts);
+    else k_count_pairs<3><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.wl, L.sc, L.cap, d_counts);
+}
+
+}  // namespace sph

@@ -1,0 +1,236 @@
+"""`solve` and the handle around the C ABI.
+
+`solve` mirrors the `solve!` methods of EtherSPHCPU.jl (src/Solve/*.jl): the wall
+argument types select the eachStep! variant exactly as Julia's dispatch does:
+
+  solve(fluid, walls, kernel, model, td, ...)                 FluidWallSolve.jl:85-140
+      walls: CompulsiveWallParticles (or any wall type)
+  solve(fluid, thermostatic_walls, kernel, thermal_model, ...) FluidThermostaticWallSolve.jl:127-173
+  solve(fluid, compulsive, thermostatic, kernel, thermal_model, ...)
+                                                              FluidCompulsiveThermostaticWallSolve.jl:154-233
+  solve(fluid, static_velocity_walls, kernel, model, ...)     FluidVelocitySolve.jl:104-168
+
+The fluid container is updated in place (positions, velocities, density, pressure,
+sound speed, temperature; particles removed by the check are dropped), like the Julia
+vector after solve!.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _abi
+from .types import (AABBCheck, CompulsiveWallParticles, StaticVelocityWallParticles, ThermostaticWallParticles,
+                    isOutputStep)
+
+
+def make_params(kernel, model, td, *, solve: int, precision: int = _abi.PRECISION_FP64, check: AABBCheck | None = None,
+                domain_lo=None, domain_hi=None, periodic_x: bool = False, nan_check: bool = True) -> _abi.SphParams:
+    """Fill the C parameter block from the Julia-mirror objects."""
+    p = _abi.SphParams()
+    p.dim = kernel.dim_
+    p.kernel = kernel.kind.code
+    p.solve = solve
+    p.precision = precision
+    p.influence_radius = kernel.influence_radius_
+    p.h = kernel.h_
+    p.sigma = kernel.sigma_
+    p.kernel_0 = kernel.kernel_0_
+    p.rho_0 = model.rho_0_
+    p.c_0 = model.c_0_
+    p.p_0 = model.p_0_
+    p.gamma = model.gamma_
+    p.thermal = 1 if model.thermal else 0
+    p.b = model.b_
+    p.mu_0 = model.mu_0_
+    p.nu_0 = model.nu_0_
+    for k in range(3):
+        p.body_force[k] = float(model.body_force_vec_[k]) if k < len(model.body_force_vec_) else 0.0
+    if model.thermal:
+        p.t_0 = model.t_0_
+        p.kappa_0 = model.kappa_0_
+        p.cp = model.cp_
+        p.beta = model.beta_
+    p.dt = td.dt_
+    p.total_step = td.total_step_
+    p.output_interval = td.output_interval_
+    p.check_interval = td.check_interval_
+    p.density_reinitialized_interval = td.density_reinitialized_interval_
+    p.check_enabled = 1 if check is not None else 0
+    chk = check or AABBCheck()
+    for k in range(3):
+        p.check_lo[k] = chk.lo[k] if k < len(chk.lo) else -math.inf
+        p.check_hi[k] = chk.hi[k] if k < len(chk.hi) else math.inf
+    for k in range(3):
+        p.domain_lo[k] = domain_lo[k] if domain_lo is not None and k < len(domain_lo) else 0.0
+        p.domain_hi[k] = domain_hi[k] if domain_hi is not None and k < len(domain_hi) else 1.0
+    p.periodic_x = 1 if periodic_x else 0
+    p.nan_check = 1 if nan_check else 0
+    return p
+
+
+class Simulation:
+    """One device-resident scene behind an ``SphHandle``."""
+
+    def __init__(self, params: _abi.SphParams, fluid_capacity: int, wall_capacity: int, lib=None):
+        self.lib = lib or _abi.load_library()
+        self.params = params
+        self.dim = params.dim
+        self.thermal = bool(params.thermal)
+        h = C.c_void_p()
+        _abi.check(self.lib, None, self.lib.sph_create(C.byref(params), fluid_capacity, max(wall_capacity, 0),
+                                                       C.byref(h)))
+        self.h = h
+
+    # -- lifetime
+    def close(self):
+        if self.h:
+            self.lib.sph_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        _abi.check(self.lib, self.h, rc)
+
+    # -- data
+    def upload_fluid(self, fluid) -> None:
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        n = len(fluid)
+        args = [f(fluid.x_vec_), f(fluid.v_vec_), f(fluid.rho_), f(fluid.p_), f(fluid.c_), f(fluid.mass_),
+                f(fluid.gap_)]
+        if self.thermal:
+            args += [f(fluid.t_), f(fluid.kappa_), f(fluid.cp_)]
+        else:
+            args += [None, None, None]
+        self._keep = args
+        self._check(self.lib.sph_upload_fluid(self.h, n, *[_abi.dptr(a) for a in args]))
+
+    def upload_walls(self, walls) -> None:
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        n = len(walls)
+        kind = walls.wall_kind
+        t = f(walls.t_) if kind == _abi.WALL_THERMOSTATIC else None
+        kap = f(walls.kappa_) if kind == _abi.WALL_THERMOSTATIC else None
+        v = f(walls.v_vec_) if kind == _abi.WALL_STATIC_VELOCITY else None
+        self._check(self.lib.sph_upload_walls(self.h, kind, n, _abi.dptr(f(walls.x_vec_)),
+                                              _abi.dptr(f(walls.normal_vec_)), _abi.dptr(f(walls.gap_)),
+                                              _abi.dptr(t), _abi.dptr(kap), _abi.dptr(v)))
+
+    def step(self, first_step: int, nsteps: int) -> None:
+        self._check(self.lib.sph_step(self.h, first_step, nsteps))
+
+    def download(self, capacity: int | None = None) -> dict:
+        cap = capacity if capacity is not None else self.stats().n_fluid
+        d = self.dim
+        out = {k: np.empty((cap, d)) for k in ("x", "v")}
+        names = ["rho", "p", "c", "mass", "gap"] + (["t", "kappa", "cp"] if self.thermal else [])
+        for k in names:
+            out[k] = np.empty(cap)
+        n = C.c_int64()
+        ptr = lambda k: _abi.dptr(out[k]) if k in out else None
+        self._check(self.lib.sph_download_fluid(self.h, cap, C.byref(n), ptr("x"), ptr("v"), ptr("rho"), ptr("p"),
+                                                ptr("c"), ptr("mass"), ptr("gap"), ptr("t"), ptr("kappa"),
+                                                ptr("cp")))
+        return {k: a[: n.value] for k, a in out.items()}
+
+    def download_into(self, fluid) -> None:
+        r = self.download(len(fluid))
+        n = len(r["rho"])
+        fluid.resize(n)
+        fluid.x_vec_[:] = r["x"]
+        fluid.v_vec_[:] = r["v"]
+        fluid.rho_[:] = r["rho"]
+        fluid.p_[:] = r["p"]
+        fluid.c_[:] = r["c"]
+        fluid.mass_[:] = r["mass"]
+        fluid.gap_[:] = r["gap"]
+        if self.thermal:
+            fluid.t_[:] = r["t"]
+
+    def stats(self) -> _abi.SphStats:
+        s = _abi.SphStats()
+        self._check(self.lib.sph_stats(self.h, C.byref(s)))
+        return s
+
+    def count_pairs(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.lib.sph_count_pairs(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.sph_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def time_stages(self, reps: int = 10) -> dict:
+        ms = np.zeros(_abi.NUM_STAGES)
+        self._check(self.lib.sph_time_stages(self.h, reps, _abi.dptr(ms)))
+        return dict(zip(_abi.STAGE_NAMES, ms.tolist()))
+
+
+def _variant(walls):
+    if len(walls) == 2:
+        return _abi.SOLVE_FLUID_COMPULSIVE_THERMOSTATIC_WALL
+    w = walls[0]
+    if isinstance(w, ThermostaticWallParticles):
+        return _abi.SOLVE_FLUID_THERMOSTATIC_WALL
+    if isinstance(w, StaticVelocityWallParticles):
+        return _abi.SOLVE_FLUID_VELOCITY_WALL
+    return _abi.SOLVE_FLUID_WALL
+
+
+def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: int = _abi.PRECISION_FP64,
+          domain_lo=None, domain_hi=None, periodic_x: bool = False, first_step: int = 1, nsteps: int | None = None):
+    """GPU counterpart of solve!(fluid, walls..., kernel, model, td, vtp_io; check).
+
+    Runs steps first_step .. td.total_step_ (or `nsteps` steps), writes VTP snapshots
+    at output steps when `vtp_io` is given, and leaves the final state in `fluid`.
+    `domain_lo/hi` bound the cell grid (default: the particles' bounding box grown by
+    two cut-off radii; particles leaving it are clamped into the edge cells, which
+    stays exact but slower).
+    """
+    *walls, kernel, model, td = args
+    for w in walls:
+        assert isinstance(w, (CompulsiveWallParticles, ThermostaticWallParticles, StaticVelocityWallParticles))
+    variant = _variant(walls)
+    if domain_lo is None or domain_hi is None:
+        pts = np.concatenate([fluid.x_vec_] + [w.x_vec_ for w in walls if len(w)])
+        pad = 2.0 * kernel.influence_radius_
+        domain_lo = pts.min(axis=0) - pad if domain_lo is None else domain_lo
+        domain_hi = pts.max(axis=0) + pad if domain_hi is None else domain_hi
+    params = make_params(kernel, model, td, solve=variant, precision=precision, check=check,
+                         domain_lo=list(domain_lo), domain_hi=list(domain_hi), periodic_x=periodic_x)
+    nw = sum(len(w) for w in walls)
+    with Simulation(params, max(len(fluid), 1), nw) as sim:
+        for w in walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(fluid)
+        if vtp_io is not None:
+            vtp_io.write(0, 0.0, fluid, walls)
+        last = td.total_step_ if nsteps is None else first_step + nsteps - 1
+        step = first_step
+        while step <= last:
+            # run up to the next output step (isOutputStep, TimeDiscretization.jl:13-18)
+            nxt = step
+            while nxt < last and not (vtp_io is not None and isOutputStep(nxt, td)):
+                nxt += 1
+            sim.step(step, nxt - step + 1)
+            step = nxt + 1
+            if vtp_io is not None and isOutputStep(nxt, td):
+                sim.download_into(fluid)
+                vtp_io.write(nxt // td.output_interval_, nxt * td.dt_, fluid, walls)
+        sim.download_into(fluid)
+    return fluid

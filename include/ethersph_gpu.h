@@ -1,0 +1,228 @@
+/*
+ * ethersph_gpu.h — C ABI of the GB300 (sm_103a) weakly-compressible SPH time step.
+ *
+ * This library is the drop-in for the hot loop of EtherSPHCPU.jl: the body of
+ * `eachStep!` (neighbour search, continuity, equation of state, momentum with
+ * pressure / viscosity / compulsive-wall / thermal terms, forward-Euler update,
+ * Shepard density re-initialisation and the out-of-domain check).  A Julia
+ * package adds `solve!` methods that marshal the particle vectors into plain
+ * arrays and `ccall` these entry points; VTP output stays on the host.
+ *
+ * Reference interfaces replaced (paths inside the EtherSPHCPU.jl project):
+ *   solve!(fluid, walls, kernel, model, td, vtp_io; check)
+ *       src/Solve/FluidWallSolve.jl:85-140
+ *       src/Solve/FluidThermostaticWallSolve.jl:127-173
+ *       src/Solve/FluidCompulsiveThermostaticWallSolve.jl:154-233
+ *       src/Solve/FluidVelocitySolve.jl:104-168
+ *   eachStep!(...)   FluidWallSolve.jl:8-83, FluidThermostaticWallSolve.jl:8-125,
+ *                    FluidCompulsiveThermostaticWallSolve.jl:8-152, FluidVelocitySolve.jl:8-102
+ *
+ * Conventions
+ *   - Every call returns an int32 status (SPH_OK = 0).  No exceptions cross the
+ *     ABI and no device trap is ever raised; sph_last_error() gives the text.
+ *   - Vectors are passed as packed dim x n column-major arrays (Julia
+ *     Matrix{Float64}(dim, n)): x[0], y[0], (z[0]), x[1], ...
+ *   - The caller owns every host array; the library copies in and out and keeps
+ *     no host pointer after a call returns.  The library owns all device memory
+ *     behind the opaque handle and frees it in sph_destroy().
+ *   - A handle is used by one host thread at a time.  Each handle owns one CUDA
+ *     stream; different handles may be driven from different threads.
+ */
+#ifndef ETHERSPH_GPU_H
+#define ETHERSPH_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------- */
+enum {
+    SPH_OK = 0,
+    SPH_ERR_ARG = 1,           /* invalid argument or parameter block              */
+    SPH_ERR_CUDA = 2,          /* a CUDA runtime call failed                        */
+    SPH_ERR_OOM = 3,           /* device allocation failed or budget exceeded       */
+    SPH_ERR_NAN = 4,           /* non-finite density / velocity / position found    */
+    SPH_ERR_GRID_OVERFLOW = 5, /* cell grid or capacity too small for the scene     */
+    SPH_ERR_TIMEOUT = 6,       /* a bounded wait gave up                            */
+    SPH_ERR_STATE = 7,         /* call out of order (e.g. step before upload)       */
+    SPH_ERR_NO_DEVICE = 8      /* no CUDA device / extension not usable             */
+};
+
+/* ---- SPHKernel: src/SPHKernel/SmoothKernel/SmoothKernel.jl:15-20 ------------------ */
+enum {
+    SPH_KERNEL_CUBIC_SPLINE = 0, /* CubicSpline.jl:39-73  */
+    SPH_KERNEL_GAUSSIAN = 1,     /* Gaussian.jl:31-56     */
+    SPH_KERNEL_WENDLAND_C2 = 2,  /* WendlandC2.jl:38-63   */
+    SPH_KERNEL_WENDLAND_C4 = 3   /* WendlandC4.jl:38-54   */
+};
+
+/* ---- which eachStep! method the step reproduces ---------------------------------- */
+enum {
+    SPH_SOLVE_FLUID_WALL = 0,                       /* FluidWallSolve.jl:8-83                       */
+    SPH_SOLVE_FLUID_THERMOSTATIC_WALL = 1,          /* FluidThermostaticWallSolve.jl:8-125          */
+    SPH_SOLVE_FLUID_COMPULSIVE_THERMOSTATIC_WALL = 2, /* FluidCompulsiveThermostaticWallSolve.jl:8-152 */
+    SPH_SOLVE_FLUID_VELOCITY_WALL = 3               /* FluidVelocitySolve.jl:8-102                  */
+};
+
+/* ---- wall particle types: src/Particle/FixedParticle/WallParticle.jl --------------- */
+enum {
+    SPH_WALL_COMPULSIVE = 0,      /* CompulsiveWallParticle      WallParticle.jl:8-19  */
+    SPH_WALL_STATIC_VELOCITY = 1, /* StaticVelocityWallParticle  WallParticle.jl:21-34 */
+    SPH_WALL_THERMOSTATIC = 2     /* ThermostaticWallParticle    WallParticle.jl:36-51 */
+};
+
+/* ---- arithmetic form of the pair sums -------------------------------------------- */
+enum {
+    SPH_PRECISION_FP64 = 0,             /* plain IEEE FP64, reference expression order */
+    SPH_PRECISION_FP32_COMPENSATED = 1  /* FP32 pair math on cell-relative positions,
+                                           Kahan-compensated sums, FP64 integration,
+                                           FP64 Shepard sums                          */
+};
+
+/*
+ * Parameter block.  Field names follow the Julia structs they are copied from:
+ *   SmoothKernel            SmoothKernel.jl:37-48 (h_, sigma_, kernel_0_, influence_radius_)
+ *   *WeaklyCompressibleLiquidModel   LiquidModel.jl:10-66
+ *   DensityReinitializedFixedTimeIntervalForwardEuler  FixedTimeIntervalDiscretization.jl:10-16
+ * The `check::Function` keyword of solve! (FluidWallSolve.jl:92) cannot run on the
+ * device; it becomes an axis-aligned box: a fluid particle is deleted at a check
+ * step when any coordinate is > check_hi or < check_lo (NaN compares false and
+ * keeps the particle, as `!check(p)` would for the dam-break check).
+ */
+typedef struct SphParams {
+    int32_t dim;        /* 2 or 3 */
+    int32_t kernel;     /* SPH_KERNEL_* */
+    int32_t solve;      /* SPH_SOLVE_* */
+    int32_t precision;  /* SPH_PRECISION_* */
+
+    /* SmoothKernel */
+    double influence_radius; /* r_cut */
+    double h;
+    double sigma;
+    double kernel_0;
+
+    /* equation model */
+    double rho_0;
+    double c_0;
+    double p_0;
+    int32_t gamma;      /* integer exponent of the Tait equation */
+    int32_t thermal;    /* 1: ThermalWeaklyCompressibleLiquidModel */
+    double b;           /* c_0^2 rho_0 / gamma */
+    double mu_0;
+    double nu_0;
+    double body_force[3];
+    double t_0;
+    double kappa_0;
+    double cp;
+    double beta;
+
+    /* time discretisation */
+    double dt;
+    int64_t total_step;
+    int64_t output_interval;
+    int64_t check_interval;
+    int64_t density_reinitialized_interval;
+
+    /* check predicate and periodicity */
+    int32_t check_enabled;
+    int32_t periodic_x;     /* 1: periodic in x with period domain_hi[0]-domain_lo[0] (new; not in the reference) */
+    double check_lo[3];
+    double check_hi[3];
+
+    /* extent of the cell grid; particles outside are clamped into the edge cells */
+    double domain_lo[3];
+    double domain_hi[3];
+
+    int32_t nan_check;      /* 1: sph_step returns SPH_ERR_NAN when a fluid state turns non-finite */
+    int32_t reserved0;
+} SphParams;
+
+typedef struct SphStats {
+    int64_t n_fluid;          /* live fluid particles */
+    int64_t n_wall;
+    int64_t steps_done;       /* steps run on this handle */
+    double total_mass;        /* FP64 sum of fluid masses */
+    double kinetic_energy;    /* FP64 sum of m |v|^2 / 2 */
+    double max_speed;
+    int32_t status_flags;     /* bit 0: non-finite state seen, bit 1: particle outside grid (clamped) */
+    int32_t reserved0;
+} SphStats;
+
+typedef struct SphHandle SphHandle;
+
+/* ABI version (SPH_ABI_VERSION). */
+int32_t sph_version(void);
+
+/* Create a single-scene handle: allocate device state for up to fluid_capacity fluid
+ * and wall_capacity wall particles.  Replaces the set-up part of solve!
+ * (FluidWallSolve.jl:94-104: InPlaceNeighborList construction). */
+int32_t sph_create(const SphParams* params, int64_t fluid_capacity, int64_t wall_capacity,
+                   SphHandle** out);
+
+/* Copy fluid particles in (replaces the state).  x, v: dim x n.  p and c may be NULL
+ * (then computed from rho with updatePressure!, UpdatePressure.jl:8-16); t, kappa, cp
+ * are read only for thermal models (ThermalLiquidParticle, LiquidParticle.jl:43-64).
+ * Particle identity is the index 0..n-1 of this call. */
+int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double* v,
+                         const double* rho, const double* p, const double* c,
+                         const double* mass, const double* gap, const double* t,
+                         const double* kappa, const double* cp);
+
+/* Append one group of static wall particles (WallParticle.jl).  normal: dim x n.
+ * t, kappa: SPH_WALL_THERMOSTATIC only; v (dim x n): SPH_WALL_STATIC_VELOCITY only. */
+int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
+                         const double* normal, const double* gap, const double* t,
+                         const double* kappa, const double* v);
+
+/* Run steps first_step .. first_step+nsteps-1 of eachStep!.  Step s re-initialises
+ * density when s % density_reinitialized_interval == 0 and applies the check when
+ * check_enabled and s % check_interval == 0 (FixedTimeIntervalDiscretization.jl:18-23,
+ * TimeDiscretization.jl:19-25).  Synchronous: returns after the last step finished. */
+int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps);
+
+/* Copy the live fluid particles out in their original order (deleted particles
+ * removed, as deleteat! leaves the Julia vector).  Any pointer may be NULL.
+ * capacity: room in the caller's arrays, in particles. */
+int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, double* x,
+                           double* v, double* rho, double* p, double* c, double* mass,
+                           double* gap, double* t, double* kappa, double* cp);
+
+/* FP64 reductions over the live fluid (mass, kinetic energy, max speed). */
+int32_t sph_stats(SphHandle* h, SphStats* out);
+
+/* Unique fluid-fluid pairs (i<j, CellListMap half-list convention) and fluid-wall
+ * pairs within r_cut at the current positions. */
+int32_t sph_count_pairs(SphHandle* h, int64_t* fluid_pairs, int64_t* wall_pairs);
+
+/* The cudaStream_t the handle launches on (for CUDA-event timing by the caller). */
+int32_t sph_get_stream(SphHandle* h, void** stream);
+
+/* Diagnostic: time each stage of one step with CUDA events on the handle's stream,
+ * `reps` times, without advancing the state (every stage reads one buffer and writes
+ * another).  ms_out receives SPH_NUM_STAGES averages in milliseconds. */
+#define SPH_NUM_STAGES 6
+enum {
+    SPH_STAGE_CELL_COUNT = 0, /* cell hash + per-cell count                */
+    SPH_STAGE_SCAN = 1,       /* exclusive scan -> cellStart                */
+    SPH_STAGE_SORT = 2,       /* stable (cell, id) placement + reorder      */
+    SPH_STAGE_CONTINUITY = 3, /* continuity gather + density + EOS          */
+    SPH_STAGE_MOMENTUM = 4,   /* momentum gather + integration              */
+    SPH_STAGE_REINIT = 5      /* Shepard density re-initialisation gather  */
+};
+int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out);
+
+/* Text of the last error on this handle (or of the last failed sph_create when h is NULL). */
+const char* sph_last_error(const SphHandle* h);
+
+/* Free all device memory of the handle. */
+int32_t sph_destroy(SphHandle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ETHERSPH_GPU_H */
