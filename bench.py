@@ -1,0 +1,337 @@
+"""Benchmark of the WCSPH time step: particle-steps/s on one GB300.
+
+Workload (default): the 2D natural-convection cavity, 256 x 256 = 65,536
+ThermalLiquidParticle + 3,108 wall particles, WendlandC2, FluidCompulsiveThermostatic-
+WallSolve, density re-initialisation every 30 steps.  A "step" is one eachStep! of
+that scene.  Under torchrun each rank steps its own replica of the scene (the scene
+does not shard; replicas are independent), so `value` is the sum over ranks.
+
+  python bench.py [--gpus N --steps K --warmup W --precision fp64|fp32c --impl ours|reference]
+
+Timing: W untimed warm-up steps, then K steps, each bracketed by CUDA events on the
+handle's stream with an L2 flush (a 512 MB write) before every step outside the
+events (the scene's state, ~9 MB, would otherwise sit in the 129 MB L2).  `e2e`
+times the C-ABI path a Julia caller uses: upload from host arrays, 100 steps (one
+output interval), download of the full state to host arrays.
+`--impl reference` times the CPU restatement of the reference's algorithm (half pair
+list with atomic scatter, OpenMP over all host cores) on the same scene.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s"
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp64", "fp32c"], default="fp64")
+    ap.add_argument("--n", type=int, default=256, help="cavity resolution (n x n fluid particles)")
+    ap.add_argument("--cpu-sample-steps", type=int, default=0, help="CPU baseline steps (0: auto, ~15 s)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(n):
+    from ethersph_gb300 import scenes
+    return scenes.natural_convection_2d(n=n)
+
+
+def config_of(scene, args, world):
+    return {
+        "workload": f"natural_convection_2d n={args.n}: {scene.n_fluid} ThermalLiquidParticle + {scene.n_wall} "
+                    "walls, WendlandC2, FluidCompulsiveThermostaticWallSolve, reinit every 30",
+        "fluid_particles": scene.n_fluid,
+        "wall_particles": scene.n_wall,
+        "form": args.precision,
+        "replicas": world,
+        "l2": "flushed before every timed step (512 MB write)",
+        "parallelism": f"replicas x{world}",
+    }
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------- CPU baseline
+def time_cpu(scene, steps, threads):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    fluid, walls = oracle.scene_arrays(scene)
+    prm = scene.params()
+    t0 = time.perf_counter()
+    oracle.run(prm, fluid, walls, 1, steps, mode=oracle.SCATTER, threads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(scene, args):
+    threads = cpu_threads()
+    steps = args.cpu_sample_steps
+    if steps <= 0:
+        probe = time_cpu(scene, 2, threads)
+        steps = int(max(3, min(300, 15.0 / max(probe / 2, 1e-3))))
+    secs = time_cpu(scene, steps, threads)
+    return {
+        "value": scene.n_fluid * steps / secs,
+        "unit": METRIC,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{steps} steps of the same scene (steps 1..{steps}), {secs:.2f} s, C++ restatement of "
+                  "EtherSPHCPU.jl eachStep! (half pair list + atomic scatter, OpenMP)",
+    }
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, index=0):
+        self.samples = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------- our arm
+def algorithmic_bytes(scene, precision):
+    """Bytes each particle's SoA elements move through the momentum kernel (read or
+    written once) for one launch: the unit of roofline.achieved."""
+    nf, nw = scene.n_fluid, scene.n_wall
+    if precision == "fp64":
+        fluid = (16 + 16 + 8 * 8) + (16 + 16 + 8 + 8 + 4 + 4)  # x v rhoc P m gap c T kappa cp | x' v' T' rho' key slot
+        wall = 16 + 16 + 16 + 8 + 8 + 8 + 4                    # x n v gap T kappa kind
+    else:
+        fluid = (16 + 16 + 16) + (16 + 16 + 8 + 8 + 4 + 4)   # float4 shadows | FP64 masters out
+        wall = 16 + 16 + 16
+    return nf * fluid + nw * wall
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import ethersph_gb300 as pkg
+    from ethersph_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    scene = workload(args.n)
+    prec = _abi.PRECISION_FP64 if args.precision == "fp64" else _abi.PRECISION_FP32_COMPENSATED
+    prm = scene.params(precision=prec)
+    sim = pkg.Simulation(prm, scene.n_fluid, scene.n_wall)
+    for w in scene.walls:
+        sim.upload_walls(w)
+    sim.upload_fluid(scene.fluid)
+    lib, h = sim.lib, sim.h
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    step = 1
+    for _ in range(args.warmup):
+        _abi.check(lib, h, lib.sph_step(h, step, 1))
+        step += 1
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    reinit_steps = 0
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                _abi.check(lib, h, lib.sph_step_async(h, step, 1))
+                ev[k][1].record(stream)
+                reinit_steps += step % scene.td.density_reinitialized_interval_ == 0
+                step += 1
+        _abi.check(lib, h, lib.sph_synchronize(h))
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = scene.n_fluid * args.steps * world / (ms_max / 1e3)
+    clocks = clk.summary()
+
+    # per-stage times (CUDA events on the handle's stream), dominant kernel roofline
+    stages = sim.time_stages(20)
+    mom_ms = stages["momentum"]
+    bytes_mom = algorithmic_bytes(scene, args.precision)
+    peaks = json.loads(MEASURED_PEAKS.read_text()) if MEASURED_PEAKS.exists() else {}
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or FALLBACK_HBM_GBS
+    achieved = bytes_mom / (mom_ms / 1e3) / 1e9
+    pairs_ff, pairs_fw = sim.count_pairs()
+
+    # e2e through the C ABI with host buffers: upload, 100 steps, download
+    r = {}
+    f = scene.fluid
+    h2d = sum(a.nbytes for a in (f.x_vec_, f.v_vec_, f.rho_, f.p_, f.c_, f.mass_, f.gap_, f.t_, f.kappa_, f.cp_))
+    e2e_steps = 100
+    e2e_iters = 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(e2e_iters):
+        sim.upload_fluid(f)
+        sim.step(1, e2e_steps)
+        r = sim.download(scene.n_fluid)
+    e2e_s = time.perf_counter() - t0
+    d2h = sum(a.nbytes for a in r.values())
+    e2e_val = scene.n_fluid * e2e_steps * e2e_iters / e2e_s
+    et = torch.tensor([e2e_val], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(et, op=torch.distributed.ReduceOp.MIN)
+    e2e_val = float(et.item()) * world
+    sim.close()
+
+    if rank != 0:
+        return None
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": METRIC,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32",
+        "data": "synthetic (seeded scene generator)",
+        "config": config_of(scene, args, world),
+        "pair_interactions_per_s": pairs_ff * args.steps * world / (ms_max / 1e3),
+        "pairs": {"fluid_fluid_unique": pairs_ff, "fluid_wall": pairs_fw},
+        "stages_ms": stages,
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "momentum (K5)",
+            "achieved": achieved,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": achieved / hbm,
+            "peak_source": f"{peak_src} hbm_gbs",
+            "algorithmic_bytes_per_launch": bytes_mom,
+            "traffic": None,
+            "note": "FP64 pair arithmetic is ALU-bound on GB300; the HBM fraction is low by design"
+            if args.precision == "fp64" else "",
+        },
+        "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps,
+                "what": f"upload + {e2e_steps} steps + download per iteration, {e2e_iters} iterations"},
+        "gpu_launches": args.steps * 7 + reinit_steps,
+        "clocks": clocks,
+    }
+    return out
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        if rank == 0:
+            scene = workload(args.n)
+            threads = cpu_threads()
+            tt = []
+            for k in range(args.warmup):
+                time_cpu(scene, 1, threads)
+            for k in range(args.steps):
+                tt.append(time_cpu(scene, 1, threads))
+            secs = sum(tt)
+            val = scene.n_fluid * args.steps / secs
+            line = {"metric": METRIC, "value": val, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
+                    "config": config_of(scene, args, 1), "impl": "reference",
+                    "cpu_baseline": {"value": val, "unit": METRIC, "cores": threads, "kind": "port",
+                                     "sample": f"{args.steps} single-step runs from the initial state of the same "
+                                               "scene; C++ restatement of EtherSPHCPU.jl eachStep! (Julia absent)"},
+                    "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line))
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    out = run_ours(args, rank, world, local)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(workload(args.n), args)
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

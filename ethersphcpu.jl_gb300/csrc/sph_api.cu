@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -200,6 +201,7 @@ struct SphHandle {
     unsigned long long* d_pair_counts = nullptr;
     int64_t* h_pinned_step = nullptr;
     int par = 0;
+    int64_t dev_step = INT64_MIN;  // value of the device step counter (host mirror)
     bool have_fluid = false;
     int64_t steps_done = 0;
     std::string err;
@@ -547,15 +549,16 @@ int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
     return SPH_OK;
 }
 
-int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps) {
+int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_step before sph_upload_fluid");
     if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
     if (nsteps == 0) return SPH_OK;
     cudaStream_t st = h->stream;
-    h->h_pinned_step[0] = first_step;
-    SPH_CUDA(h, cudaMemcpyAsync(h->sc.scene_step, h->h_pinned_step, 8, cudaMemcpyHostToDevice, st));
-    SPH_CUDA(h, cudaMemsetAsync(h->sc.status, 0, 4, st));
+    if (first_step != h->dev_step) {  // the device step counter only needs a reset on a jump
+        h->h_pinned_step[0] = first_step;
+        SPH_CUDA(h, cudaMemcpyAsync(h->sc.scene_step, h->h_pinned_step, 8, cudaMemcpyHostToDevice, st));
+    }
     const int64_t bundle = 10;
     int64_t s = first_step;
     const int64_t end = first_step + nsteps;
@@ -587,14 +590,28 @@ int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps) {
         if (nb & 1) h->par ^= 1;
         s += nb;
     }
-    int32_t status = 0;
-    SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned_step[1], h->sc.status, 4, cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    std::memcpy(&status, &h->h_pinned_step[1], 4);
+    h->dev_step = end;
     h->steps_done += nsteps;
+    return SPH_OK;
+}
+
+int32_t sph_synchronize(SphHandle* h) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    cudaStream_t st = h->stream;
+    SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned_step[1], h->sc.status, 4, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(h, cudaMemsetAsync(h->sc.status, 0, 4, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    int32_t status = 0;
+    std::memcpy(&status, &h->h_pinned_step[1], 4);
     if ((status & kStatusNonFinite) && h->prm.nan_check)
         return fail(h, SPH_ERR_NAN, "non-finite fluid state (density, velocity or position)");
     return SPH_OK;
+}
+
+int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps) {
+    int32_t rc = sph_step_async(h, first_step, nsteps);
+    if (rc != SPH_OK) return rc;
+    return sph_synchronize(h);
 }
 
 int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, double* x, double* v, double* rho,

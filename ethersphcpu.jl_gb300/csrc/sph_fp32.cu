@@ -1,7 +1,473 @@
-// sph_fp32.cu — FP32-compensated form of the gather kernels (work in progress: the
-// engine rejects SPH_PRECISION_FP32_COMPENSATED until these kernels exist).
+// sph_fp32.cu — FP32-compensated form of the continuity and momentum gathers.
+//
+// Pair arithmetic runs in FP32 on cell-relative positions: every particle carries
+// (x - origin of its cell) as floats, and a neighbour in the cell offset (dx, dy, dz)
+// sits at xr_j + (dx, dy, dz) * edge in the frame of particle i's cell, so r_vec is
+// formed from numbers of magnitude <= 2 r_cut with an absolute error of a few 1e-9 r_cut.
+// The continuity and force sums are Kahan-compensated FP32 accumulators; the result
+// (sum - compensation) is taken to FP64 before the forward-Euler update, which runs in
+// FP64 on the FP64 master position / velocity / density / temperature.  The Shepard
+// re-initialisation keeps its FP64 kernel (sph_fp64.cu).
+//
+// Same terms, order of walls after fluid, and solve variants as sph_fp64.cu; the
+// formulas follow Continuity.jl, PressureForce.jl, ViscosityForce.jl, WallForce.jl,
+// ThermalConduction.jl and SelfAction/*.jl.
+#include "sph_physics.cuh"
 #include "sph_kernels.h"
 
 namespace sph {
-void launch_physics_fp32(int, const LaunchCtx&) {}
+
+namespace {
+
+enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2 };
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// W and dW/dr in FP32 (same polynomials as sph_physics.cuh).
+template <int KK>
+__device__ __forceinline__ void kernel_wdw_f(float q, const SceneDev& S, float& W, float& dW) {
+    if (KK == SPH_KERNEL_CUBIC_SPLINE) {
+        if (q < 1.f) {
+            W = S.kw_a_f * (3.f * q * q * (q - 2.f) + 4.f);
+            dW = S.kg_a_f * q * (3.f * q - 4.f);
+        } else if (q < 2.f) {
+            const float t = 2.f - q;
+            W = S.kw_a_f * t * t * t;
+            dW = -S.kg_a_f * t * t;
+        } else {
+            W = 0.f;
+            dW = 0.f;
+        }
+    } else if (KK == SPH_KERNEL_GAUSSIAN) {
+        if (q < 3.f) {
+            const float e = __expf(-q * q);
+            W = S.kw_a_f * e;
+            dW = S.kg_a_f * q * e;
+        } else {
+            W = 0.f;
+            dW = 0.f;
+        }
+    } else if (KK == SPH_KERNEL_WENDLAND_C2) {
+        if (q < 2.f) {
+            const float t = 2.f - q;
+            const float t3 = t * t * t;
+            W = S.kw_a_f * (t3 * t) * (1.f + 2.f * q) * 0.0625f;
+            dW = S.kg_a_f * q * t3;
+        } else {
+            W = 0.f;
+            dW = 0.f;
+        }
+    } else {
+        if (q < 2.f) {
+            const float t = 2.f - q;
+            const float t2 = t * t;
+            const float t5 = t2 * t2 * t;
+            W = S.kw_a_f * (t5 * t) * (35.f * q * q + 36.f * q + 12.f) * (1.f / 768.f);
+            dW = S.kg_a_f * (35.f / 96.f * q * q + 7.f / 48.f * q) * t5;
+        } else {
+            W = 0.f;
+            dW = 0.f;
+        }
+    }
+}
+
+template <int KK>
+__device__ __forceinline__ float kernel_w_f(float q, const SceneDev& S) {
+    float W, dW;
+    kernel_wdw_f<KK>(q, S, W, dW);
+    return W;
+}
+
+// Visits the neighbour cells one by one (z, y, x order), handing the callback the
+// cell's sorted range and its offset from particle i's cell in metres.
+template <int DIM, typename F>
+__device__ __forceinline__ void walk_cells_rel(const SceneDev& S, const int32_t* __restrict__ start,
+                                               const int32_t c[3], F&& f) {
+    const int zr = DIM == 3 ? 1 : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const int z = c[2] + dz;
+        if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = c[1] + dy;
+            if (y < 0 || y >= S.n[1]) continue;
+            const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
+            for (int dx = -1; dx <= 1; ++dx) {
+                int x = c[0] + dx;
+                if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
+                else if (x < 0 || x >= S.n[0]) continue;
+                const float ox = (float)dx * S.cell_f[0];
+                const float oy = (float)dy * S.cell_f[1];
+                const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
+                f(__ldg(start + row + x), __ldg(start + row + x + 1), ox, oy, oz);
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------------- K4 (FP32)
+template <int DIM, int KK>
+__global__ void __launch_bounds__(128) k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st,
+                                                        const int32_t* __restrict__ start,
+                                                        const int32_t* __restrict__ n_live, int32_t cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *n_live) return;
+    const SceneDev& S = scenes[st.scene[i]];
+    const float4 ai = st.fa[i];
+    const float4 bi = st.fb[i];
+    float xi[3], vi[3];
+    if (DIM == 2) {
+        xi[0] = ai.x; xi[1] = ai.y; xi[2] = 0.f;
+        vi[0] = ai.z; vi[1] = ai.w; vi[2] = 0.f;
+    } else {
+        xi[0] = ai.x; xi[1] = ai.y; xi[2] = ai.z;
+        vi[0] = bi.x; vi[1] = bi.y; vi[2] = bi.z;
+    }
+    int32_t c[3];
+    {
+        const int32_t key = st.cell[i] - S.cell_off;
+        c[0] = key % S.n[0];
+        c[1] = (key / S.n[0]) % S.n[1];
+        c[2] = key / (S.n[0] * S.n[1]);
+    }
+    Kahan drho;
+    walk_cells_rel<DIM>(S, start, c, [&](int jb, int je, float ox, float oy, float oz) {
+        const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            const float4 aj = st.fa[j];
+            const float rx = bx - aj.x, ry = by - aj.y;
+            const float rz = DIM == 3 ? bz - aj.z : 0.f;
+            const float d2 = rx * rx + ry * ry + rz * rz;
+            if (!(d2 <= S.rc2_f) || d2 == 0.f) continue;
+            const float inv_r = rsqrtf(d2);
+            const float r = d2 * inv_r;
+            float W, dW;
+            kernel_wdw_f<KK>(r * S.inv_h_f, S, W, dW);
+            const float s = dW * inv_r;
+            float vx, vy, vz, mj;
+            if (DIM == 2) {
+                vx = vi[0] - aj.z;
+                vy = vi[1] - aj.w;
+                vz = 0.f;
+                mj = st.fb[j].x;
+            } else {
+                const float4 bj = st.fb[j];
+                vx = vi[0] - bj.x;
+                vy = vi[1] - bj.y;
+                vz = vi[2] - bj.z;
+                mj = aj.w;
+            }
+            drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
+        }
+    });
+    double rho = st.rho[i];
+    rho += drho.value() * S.dt;
+    const double rr = rho / S.rho0;
+    const double p = S.b * (jl_powi(rr, S.gamma) - 1.0) + S.p0;
+    const double cs = S.c0 * sqrt(jl_powi(rr, S.gamma - 1));
+    const double P = p / (rho * rho);
+    st.rhoc[i] = rho;
+    st.p[i] = p;
+    st.c[i] = cs;
+    st.P[i] = P;
+    if (DIM == 2) {
+        st.fb[i] = make_float4(bi.x, (float)rho, (float)P, bi.w);
+    } else {
+        st.fb[i] = make_float4(bi.x, bi.y, bi.z, (float)rho);
+        const float4 ci = st.fc[i];
+        st.fc[i] = make_float4((float)P, ci.y, ci.z, ci.w);
+    }
+}
+
+// -------------------------------------------------------------------- K5 (FP32)
+template <int DIM, int KK, int MODE>
+__global__ void __launch_bounds__(128) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st,
+                                                      NextState nx, WallState wl, SortScratch sc, int32_t cap) {
+    using V = typename VecT<DIM>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    const int64_t step = sc.scene_step[s];
+    const float4 ai = st.fa[i];
+    const float4 bi = st.fb[i];
+    float xi[3], vi[3], m_i, rho_i, P_i, gap_i;
+    float T_i = 0.f, kap_i = 0.f, cp_i = 1.f;
+    if (DIM == 2) {
+        xi[0] = ai.x; xi[1] = ai.y; xi[2] = 0.f;
+        vi[0] = ai.z; vi[1] = ai.w; vi[2] = 0.f;
+        m_i = bi.x; rho_i = bi.y; P_i = bi.z; gap_i = bi.w;
+        if (MODE == kModeThermal) {
+            const float4 ci = st.fc[i];
+            T_i = ci.x; kap_i = ci.y; cp_i = ci.z;
+        }
+    } else {
+        xi[0] = ai.x; xi[1] = ai.y; xi[2] = ai.z; m_i = ai.w;
+        vi[0] = bi.x; vi[1] = bi.y; vi[2] = bi.z; rho_i = bi.w;
+        const float4 ci = st.fc[i];
+        P_i = ci.x; gap_i = ci.y;
+        if (MODE == kModeThermal) {
+            T_i = ci.z; kap_i = ci.w; cp_i = st.fd[i];
+        }
+    }
+    const float c_i = (float)st.c[i];
+    const float mu_i = S.nu0_f * rho_i;
+    const float inv_h = S.inv_h_f;
+    const float inv_Wg_i = 1.f / kernel_w_f<KK>(gap_i * inv_h, S);
+    const float inv_cp_i = 1.f / cp_i;
+    int32_t c[3];
+    {
+        const int32_t key = st.cell[i] - S.cell_off;
+        c[0] = key % S.n[0];
+        c[1] = (key / S.n[0]) % S.n[1];
+        c[2] = key / (S.n[0] * S.n[1]);
+    }
+    Kahan dv[3], dT;
+
+    walk_cells_rel<DIM>(S, sc.start, c, [&](int jb, int je, float ox, float oy, float oz) {
+        const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
+        for (int j = jb; j < je; ++j) {
+            if (j == i) continue;
+            const float4 aj = st.fa[j];
+            const float rx = bx - aj.x, ry = by - aj.y;
+            const float rz = DIM == 3 ? bz - aj.z : 0.f;
+            const float d2 = rx * rx + ry * ry + rz * rz;
+            if (!(d2 <= S.rc2_f) || d2 == 0.f) continue;
+            const float inv_r = rsqrtf(d2);
+            const float r = d2 * inv_r;
+            float W, dW;
+            kernel_wdw_f<KK>(r * inv_h, S, W, dW);
+            const float4 bj = st.fb[j];
+            float vx, vy, vz, m_j, rho_j, P_j, gap_j;
+            float T_j = 0.f, kap_j = 0.f;
+            if (DIM == 2) {
+                vx = vi[0] - aj.z; vy = vi[1] - aj.w; vz = 0.f;
+                m_j = bj.x; rho_j = bj.y; P_j = bj.z; gap_j = bj.w;
+                if (MODE == kModeThermal) {
+                    const float4 cj = st.fc[j];
+                    T_j = cj.x; kap_j = cj.y;
+                }
+            } else {
+                vx = vi[0] - bj.x; vy = vi[1] - bj.y; vz = vi[2] - bj.z;
+                m_j = aj.w; rho_j = bj.w;
+                const float4 cj = st.fc[j];
+                P_j = cj.x; gap_j = cj.y;
+                if (MODE == kModeThermal) {
+                    T_j = cj.z; kap_j = cj.w;
+                }
+            }
+            // pressure (PressureForce.jl:14-19), tensile term included
+            float prho2 = P_i + P_j;
+            const float inv_Wg = S.uniform_gap ? inv_Wg_i : 1.f / kernel_w_f<KK>(0.5f * (gap_i + gap_j) * inv_h, S);
+            prho2 += fabsf(prho2) * 0.01f * W * inv_Wg;
+            // viscosity (ViscosityForce.jl:15-23)
+            const float sum_rho = rho_i + rho_j;
+            const float f = 4.f * (mu_i + S.nu0_f * rho_j) * r * dW / (sum_rho * sum_rho * (r * r + S.hh001_f));
+            const float gp = -m_j * prho2 * dW * inv_r;  // pressure term along r_vec
+            const float gv = m_j * f;                    // viscosity term along v_ij
+            dv[0].add(gp * rx + gv * vx);
+            dv[1].add(gp * ry + gv * vy);
+            if (DIM == 3) dv[2].add(gp * rz + gv * vz);
+            if (MODE == kModeThermal) {  // ThermalConduction.jl:15-21
+                const float keq = 2.f * kap_i * kap_j / (kap_i + kap_j);
+                const float dq = 2.f * keq * r * dW / (rho_i * rho_j * (r * r + S.hh001_f)) * (T_i - T_j);
+                dT.add(dq * m_j * inv_cp_i);
+            }
+        }
+    });
+
+    if (wl.n > 0) {
+        walk_cells_rel<DIM>(S, wl.start, c, [&](int jb, int je, float ox, float oy, float oz) {
+            const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
+            for (int w = jb; w < je; ++w) {
+                const float4 wa = wl.fa[w];
+                const float4 wb = wl.fb[w];
+                float rv[3], n[3], vv[3], gw, Tw = 0.f, kw = 0.f;
+                bool thermo = false;
+                if (DIM == 2) {
+                    rv[0] = bx - wa.x; rv[1] = by - wa.y; rv[2] = 0.f;
+                    n[0] = wa.z; n[1] = wa.w; n[2] = 0.f;
+                    vv[0] = vi[0] - wb.x; vv[1] = vi[1] - wb.y; vv[2] = 0.f;
+                    gw = wb.z;
+                    if (MODE == kModeThermal) {
+                        const float4 wc = wl.fc[w];
+                        Tw = wb.w; kw = wc.x; thermo = wc.y != 0.f;
+                    }
+                } else {
+                    rv[0] = bx - wa.x; rv[1] = by - wa.y; rv[2] = bz - wa.z;
+                    gw = wa.w;
+                    n[0] = wb.x; n[1] = wb.y; n[2] = wb.z;
+                    const float4 wc = wl.fc[w];
+                    vv[0] = vi[0] - wc.x; vv[1] = vi[1] - wc.y; vv[2] = vi[2] - wc.z;
+                    if (MODE == kModeThermal) {
+                        Tw = wb.w; kw = wc.w; thermo = wl.kind[w] == SPH_WALL_THERMOSTATIC;
+                    }
+                }
+                const float d2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+                if (!(d2 <= S.rc2_f)) continue;
+                const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+                const float r = d2 * inv_r;
+                float W, dW;
+                kernel_wdw_f<KK>(r * inv_h, S, W, dW);
+                const float vert = vv[0] * n[0] + vv[1] * n[1] + vv[2] * n[2];
+                float acc[3] = {0.f, 0.f, 0.f};
+                {  // WallForce.jl:15-28
+                    const float psi = fabsf(rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2]);
+                    const float xi_ = sqrtf(fmaxf(r * r - psi * psi, 0.f));
+                    const float q = psi / gw;
+                    if (!(q > 1.f || xi_ > gw)) {
+                        const float pxi = fabsf((1.f + cospif(xi_ / gw)) * 0.5f);
+                        const float beta = vert > 0.f ? 0.f : 1.f;
+                        const float rpsi = (0.01f * c_i * c_i + beta * c_i * fabsf(vert)) * inv_h * fabsf(1.f - q) *
+                                           rsqrtf(q);
+                        const float wf = rpsi * pxi;
+                        acc[0] += wf * n[0];
+                        acc[1] += wf * n[1];
+                        acc[2] += wf * n[2];
+                    }
+                }
+                if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
+                    float prho2 = P_i + S.P_bg_f;
+                    prho2 += fabsf(prho2) * 0.01f * W * inv_Wg_i;
+                    const float gp = -m_i * prho2 * dW * inv_r;
+                    acc[0] += gp * rv[0];
+                    acc[1] += gp * rv[1];
+                    acc[2] += gp * rv[2];
+                }
+                {  // ViscosityForce.jl:34-44
+                    const float sum_rho = 2.f * rho_i;
+                    const float f = 8.f * mu_i * r * dW / (sum_rho * sum_rho * (r * r + S.hh001_f));
+                    const float gv = m_i * f;
+                    acc[0] += gv * (vv[0] - vert * n[0]);
+                    acc[1] += gv * (vv[1] - vert * n[1]);
+                    acc[2] += gv * (vv[2] - vert * n[2]);
+                }
+                dv[0].add(acc[0]);
+                dv[1].add(acc[1]);
+                if (DIM == 3) dv[2].add(acc[2]);
+                if (MODE == kModeThermal && thermo) {  // ThermalConduction.jl:31-35
+                    const float dq = S.inv_cp_f * (kap_i + kw) * r * dW * S.inv_rho0_f /
+                                     (rho_i * (r * r + S.hh001_f)) * (T_i - Tw);
+                    dT.add(dq * m_i);
+                }
+            }
+        });
+    }
+
+    // ---- FP64 forward Euler on the masters (UpdateTemperature/Velocity/Position.jl)
+    const V* __restrict__ xm = (const V*)st.x;
+    const V* __restrict__ vm = (const V*)st.v;
+    const V x0 = xm[i];
+    const V v0 = vm[i];
+    const double dt = S.dt;
+    double dvd[DIM];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) dvd[k] = dv[k].value();
+    double body[DIM];
+    if (MODE == kModeThermal) {
+        const double Tn = st.T[i] + dt * dT.value();
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) body[k] = S.bous[k] * (Tn - S.t0);
+        nx.T[i] = Tn;
+    } else {
+        if (nx.T) nx.T[i] = st.T[i];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) body[k] = S.g[k];
+    }
+    double vn[DIM], xn[DIM];
+    vn[0] = v0.x; vn[1] = v0.y;
+    xn[0] = x0.x; xn[1] = x0.y;
+    if (DIM == 3) {
+        vn[DIM - 1] = comp(v0, DIM - 1);
+        xn[DIM - 1] = comp(x0, DIM - 1);
+    }
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        vn[k] += body[k] * dt;
+        vn[k] += dvd[k] * dt;
+        xn[k] += vn[k] * dt - dvd[k] * S.dtdt / 2.0;
+    }
+    if (S.periodic_x) {
+        if (xn[0] >= S.wrap_hi) xn[0] -= S.period;
+        else if (xn[0] < S.lo[0]) xn[0] += S.period;
+    }
+    V xo, vo;
+    xo.x = xn[0]; xo.y = xn[1];
+    vo.x = vn[0]; vo.y = vn[1];
+    if constexpr (DIM == 3) {
+        xo.z = xn[2]; xo.w = 0.0;
+        vo.z = vn[2]; vo.w = 0.0;
+    }
+    ((V*)nx.x)[i] = xo;
+    ((V*)nx.v)[i] = vo;
+    const double rho_d = st.rhoc[i];
+    nx.rho[i] = rho_d;
+
+    bool finite = isfinite(rho_d);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) finite &= isfinite(xn[k]) & isfinite(vn[k]);
+    if (!finite && S.nan_check) atomicOr(sc.status, kStatusNonFinite);
+    bool dead = false;
+    if (S.check_enabled && is_step(step, S.check_interval)) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) dead |= (xn[k] > S.check_hi[k]) | (xn[k] < S.check_lo[k]);
+    }
+    if (dead) {
+        sc.key[i] = kDeadKey;
+    } else {
+        const int32_t key = cell_key<DIM>(xo, S);
+        sc.key[i] = key;
+        sc.slot[i] = atomicAdd(sc.count + key, 1);
+    }
+}
+
+template <int DIM, int KK>
+void launch_k4(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_continuity_f32<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+}
+template <int DIM, int KK, int MODE>
+void launch_k5(const LaunchCtx& L) {
+    const int grid = (L.cap + 127) / 128;
+    k_momentum_f32<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap);
+}
+
+template <int DIM>
+void dispatch(int kk, int stage, int mode, const LaunchCtx& L) {
+#define SPH_KK_CASE(KKV)                                                              \
+    case KKV:                                                                         \
+        if (stage == 0) launch_k4<DIM, KKV>(L);                                       \
+        else if (mode == kModeFluidWall) launch_k5<DIM, KKV, kModeFluidWall>(L);      \
+        else if (mode == kModeWallPressure) launch_k5<DIM, KKV, kModeWallPressure>(L); \
+        else launch_k5<DIM, KKV, kModeThermal>(L);                                    \
+        break;
+    switch (kk) {
+        SPH_KK_CASE(SPH_KERNEL_CUBIC_SPLINE)
+        SPH_KK_CASE(SPH_KERNEL_GAUSSIAN)
+        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C2)
+        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C4)
+    }
+#undef SPH_KK_CASE
+}
+
+}  // namespace
+
+void launch_physics_fp32(int stage, const LaunchCtx& L) {
+    if (stage == 2) {  // Shepard sums stay FP64
+        launch_physics_fp64(2, L);
+        return;
+    }
+    if (L.dim == 2) dispatch<2>(L.kernel, stage, L.mode, L);
+    else dispatch<3>(L.kernel, stage, L.mode, L);
+}
+
 }  // namespace sph

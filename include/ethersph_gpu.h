@@ -184,6 +184,12 @@ int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
  * TimeDiscretization.jl:19-25).  Synchronous: returns after the last step finished. */
 int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps);
 
+/* Enqueue the same steps on the handle's stream and return without waiting (for
+ * callers that overlap host work or time the stream with CUDA events).  Status bits
+ * accumulate until sph_synchronize(), which waits and reports them like sph_step. */
+int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps);
+int32_t sph_synchronize(SphHandle* h);
+
 /* Copy the live fluid particles out in their original order (deleted particles
  * removed, as deleteat! leaves the Julia vector).  Any pointer may be NULL.
  * capacity: room in the caller's arrays, in particles. */
