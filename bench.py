@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp64", "fp32c"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp32c"], default="fp32c")
+    ap.add_argument("--fp64-steps", type=int, default=20, help="steps of the plain FP64 form reported beside")
     ap.add_argument("--n", type=int, default=256, help="cavity resolution (n x n fluid particles)")
     ap.add_argument("--cpu-sample-steps", type=int, default=0, help="CPU baseline steps (0: auto, ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -173,6 +174,37 @@ def algorithmic_bytes(scene, precision):
     return nf * fluid + nw * wall
 
 
+def time_form(pkg, _abi, scene, precision, steps, warmup, local):
+    """Plain device timing of one form (CUDA events around each step, L2 flushed)."""
+    import torch
+    prm = scene.params(precision=precision)
+    with pkg.Simulation(prm, scene.n_fluid, scene.n_wall) as sim:
+        for w in scene.walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(scene.fluid)
+        lib, h = sim.lib, sim.h
+        stream = torch.cuda.ExternalStream(sim.stream())
+        flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        step = 1
+        for _ in range(warmup):
+            _abi.check(lib, h, lib.sph_step(h, step, 1))
+            step += 1
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(stream):
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                _abi.check(lib, h, lib.sph_step_async(h, step, 1))
+                ev[k][1].record(stream)
+                step += 1
+        _abi.check(lib, h, lib.sph_synchronize(h))
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        stages = sim.time_stages(10)
+    return ms, stages
+
+
 def run_ours(args, rank, world, local):
     import torch
     import ethersph_gb300 as pkg
@@ -251,6 +283,12 @@ def run_ours(args, rank, world, local):
     e2e_val = float(et.item()) * world
     sim.close()
 
+    other = None
+    if args.precision == "fp32c" and args.fp64_steps > 0:
+        ms64, st64 = time_form(pkg, _abi, scene, _abi.PRECISION_FP64, args.fp64_steps, 2, local)
+        other = {"form": "plain fp64 (bit-exact with the CPU restatement)", "ms_per_step": ms64,
+                 "value": scene.n_fluid * world / (ms64 / 1e3), "stages_ms": st64,
+                 "speedup_of_fp32c": (scene.n_fluid * world / (ms64 / 1e3)) and value / (scene.n_fluid * world / (ms64 / 1e3))}
     if rank != 0:
         return None
     out = {
@@ -286,6 +324,7 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
                 "what": f"upload + {e2e_steps} steps + download per iteration, {e2e_iters} iterations"},
+        "plain_fp64": other,
         "gpu_launches": args.steps * 7 + reinit_steps,
         "clocks": clocks,
     }

@@ -96,10 +96,12 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
             const double L = p.domain_hi[0] - p.domain_lo[0];
             na = (int64_t)std::floor(L / edge);
             if (na < 3) { err = "a periodic axis needs at least 3 cells of edge r_cut"; return false; }
-            S.inv_cell[a] = 1.0 / (L / (double)na);
+            S.cell_d[a] = L / (double)na;
+            S.inv_cell[a] = 1.0 / S.cell_d[a];
         } else {
             na = (int64_t)std::ceil((p.domain_hi[a] - p.domain_lo[a]) / edge);
             if (na < 1) na = 1;
+            S.cell_d[a] = edge;
             S.inv_cell[a] = 1.0 / edge;
         }
         if (na > (1 << 24)) { err = "cell grid too large"; return false; }
@@ -153,7 +155,7 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.reinit_interval = p.density_reinitialized_interval;
     S.check_interval = p.check_interval;
 
-    for (int a = 0; a < 3; ++a) S.cell_f[a] = S.inv_cell[a] > 0.0 ? (float)(1.0 / S.inv_cell[a]) : 0.0f;
+    for (int a = 0; a < 3; ++a) S.cell_f[a] = (float)S.cell_d[a];
     S.h_f = (float)p.h;
     S.rc2_f = (float)(rc * rc);
     S.hh001_f = (float)S.hh001;
@@ -262,6 +264,13 @@ cudaError_t alloc_sorted(SphHandle* h, SortedState& s) {
     }
     if ((e = dalloc(h, &s.id, n)) != cudaSuccess) return e;
     if ((e = dalloc(h, &s.scene, n)) != cudaSuccess) return e;
+    if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {  // FP32 shadows of the gathers
+        if ((e = dalloc(h, &s.fa, n)) != cudaSuccess) return e;
+        if ((e = dalloc(h, &s.fb, n)) != cudaSuccess) return e;
+        if ((e = dalloc(h, &s.fc, n)) != cudaSuccess) return e;
+        if ((e = dalloc(h, &s.fd, n)) != cudaSuccess) return e;
+        if ((e = dalloc(h, &s.cell, n)) != cudaSuccess) return e;
+    }
     return cudaSuccess;
 }
 
@@ -337,8 +346,6 @@ int32_t sph_create(const SphParams* params, int64_t fluid_capacity, int64_t wall
     SceneDev S;
     std::string err;
     if (!build_scene(*params, S, err)) return fail(nullptr, SPH_ERR_ARG, err);
-    if (params->precision == SPH_PRECISION_FP32_COMPENSATED)
-        return fail(nullptr, SPH_ERR_ARG, "the FP32-compensated form is not available in this build");
 
     SphHandle* h = new SphHandle();
     h->prm = *params;
@@ -541,6 +548,47 @@ int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
         SPH_CUDA(h, cudaMemcpyAsync(h->W.kind, bkind.data(), nw * 4, cudaMemcpyHostToDevice, st));
     }
     SPH_CUDA(h, cudaMemcpyAsync(h->W.start, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st));
+    std::vector<float4> fa, fb, fc;
+    if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
+        // FP32 wall shadows, positions relative to the origin of the wall's cell
+        const SceneDev& S = h->scene;
+        if (!h->W.fa) {
+            const size_t cap = (size_t)std::max<int64_t>(h->wcap, 1);
+            SPH_CUDA(h, dalloc(h, &h->W.fa, cap));
+            SPH_CUDA(h, dalloc(h, &h->W.fb, cap));
+            SPH_CUDA(h, dalloc(h, &h->W.fc, cap));
+        }
+        fa.resize(nw);
+        fb.resize(nw);
+        fc.resize(nw);
+        for (int64_t q = 0; q < nw; ++q) {
+            const int64_t w = order[q];
+            const int32_t k = key[w] - S.cell_off;
+            const int32_t cc[3] = {k % S.n[0], (k / S.n[0]) % S.n[1], k / (S.n[0] * S.n[1])};
+            float xr[3] = {0.f, 0.f, 0.f}, nr[3] = {0.f, 0.f, 0.f}, vr[3] = {0.f, 0.f, 0.f};
+            for (int a = 0; a < dim; ++a) {
+                xr[a] = (float)(h->hwx[w * dim + a] - (S.lo[a] + (double)cc[a] * S.cell_d[a]));
+                nr[a] = (float)h->hwn[w * dim + a];
+                vr[a] = (float)h->hwv[w * dim + a];
+            }
+            const float g = (float)h->hwgap[w], T = (float)h->hwT[w], kap = (float)h->hwkappa[w];
+            const float thermo = h->hwkind[w] == SPH_WALL_THERMOSTATIC ? 1.f : 0.f;
+            if (dim == 2) {
+                fa[q] = make_float4(xr[0], xr[1], nr[0], nr[1]);
+                fb[q] = make_float4(vr[0], vr[1], g, T);
+                fc[q] = make_float4(kap, thermo, 0.f, 0.f);
+            } else {
+                fa[q] = make_float4(xr[0], xr[1], xr[2], g);
+                fb[q] = make_float4(nr[0], nr[1], nr[2], T);
+                fc[q] = make_float4(vr[0], vr[1], vr[2], kap);
+            }
+        }
+        if (nw > 0) {
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fa, fa.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fb, fb.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fc, fc.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+        }
+    }
     SPH_CUDA(h, cudaStreamSynchronize(st));
     h->W.n = nw;
     // the captured graphs hold the old wall state

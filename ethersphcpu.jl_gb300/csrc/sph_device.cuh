@@ -31,6 +31,7 @@ struct SceneDev {
     // cell grid
     double lo[3];
     double inv_cell[3];
+    double cell_d[3];   // cell edge per axis; cell c starts at lo + c * cell_d
     int32_t n[3];
     int32_t cell_off;   // first global cell of this scene
     int32_t ncells;

@@ -162,8 +162,9 @@ __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t c
     sc.tmp[sc.start[key] + sc.slot[i]] = id[i];
 }
 
-template <int DIM, bool THERMAL>
-__global__ void k_place(SortedState src, NextState nx, SortedState dst, SortScratch sc, int32_t cap) {
+template <int DIM, bool THERMAL, bool SHADOW>
+__global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, NextState nx, SortedState dst,
+                        SortScratch sc, int32_t cap) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
@@ -187,6 +188,34 @@ __global__ void k_place(SortedState src, NextState nx, SortedState dst, SortScra
         dst.T[d] = nx.T[i];
         dst.kappa[d] = src.kappa[i];
         dst.cp[d] = src.cp[i];
+    }
+    if (SHADOW) {  // FP32 shadows: position relative to the origin of the particle's cell
+        const SceneDev& S = scenes[src.scene[i]];
+        const int32_t k = key - S.cell_off;
+        const int32_t cx = k % S.n[0], cy = (k / S.n[0]) % S.n[1], cz = k / (S.n[0] * S.n[1]);
+        const V x = ((const V*)nx.x)[i];
+        const V v = ((const V*)nx.v)[i];
+        const float xr = (float)(x.x - __dadd_rn(S.lo[0], __dmul_rn((double)cx, S.cell_d[0])));
+        const float yr = (float)(x.y - __dadd_rn(S.lo[1], __dmul_rn((double)cy, S.cell_d[1])));
+        const float m = (float)src.m[i], rho = (float)nx.rho[i], gap = (float)src.gap[i];
+        float T = 0.f, kap = 0.f, cpv = 1.f;
+        if (THERMAL) {
+            T = (float)nx.T[i];
+            kap = (float)src.kappa[i];
+            cpv = (float)src.cp[i];
+        }
+        dst.cell[d] = key;
+        if constexpr (DIM == 2) {
+            dst.fa[d] = make_float4(xr, yr, (float)v.x, (float)v.y);
+            dst.fb[d] = make_float4(m, rho, 0.f, gap);
+            dst.fc[d] = make_float4(T, kap, cpv, 0.f);
+        } else {
+            const float zr = (float)(x.z - __dadd_rn(S.lo[2], __dmul_rn((double)cz, S.cell_d[2])));
+            dst.fa[d] = make_float4(xr, yr, zr, m);
+            dst.fb[d] = make_float4((float)v.x, (float)v.y, (float)v.z, rho);
+            dst.fc[d] = make_float4(0.f, gap, T, kap);
+            dst.fd[d] = cpv;
+        }
     }
 }
 
@@ -294,13 +323,16 @@ void launch_scan(const LaunchCtx& L, int advance) {
 void launch_place(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
     k_fill<<<grid, 128, 0, L.stream>>>(L.sc, L.st.id, L.cap);
+#define SPH_PLACE(D, T, SH) k_place<D, T, SH><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.st2, L.sc, L.cap)
+    const bool sh = L.precision == SPH_PRECISION_FP32_COMPENSATED;
     if (L.dim == 2) {
-        if (L.thermal) k_place<2, true><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
-        else k_place<2, false><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+        if (L.thermal) { if (sh) SPH_PLACE(2, true, true); else SPH_PLACE(2, true, false); }
+        else { if (sh) SPH_PLACE(2, false, true); else SPH_PLACE(2, false, false); }
     } else {
-        if (L.thermal) k_place<3, true><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
-        else k_place<3, false><<<grid, 128, 0, L.stream>>>(L.st, L.nx, L.st2, L.sc, L.cap);
+        if (L.thermal) { if (sh) SPH_PLACE(3, true, true); else SPH_PLACE(3, true, false); }
+        else { if (sh) SPH_PLACE(3, false, true); else SPH_PLACE(3, false, false); }
     }
+#undef SPH_PLACE
 }
 
 void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out) {
