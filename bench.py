@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--n", type=int, default=256, help="cavity resolution (n x n fluid particles)")
     ap.add_argument("--cpu-sample-steps", type=int, default=0, help="CPU baseline steps (0: auto, ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-steps", action="store_true",
+                    help="upload, warm up and run the timed steps only (the command profiled with ncu)")
     return ap.parse_args()
 
 
@@ -243,6 +245,11 @@ def run_ours(args, rank, world, local):
         _abi.check(lib, h, lib.sph_synchronize(h))
         torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev)
+    if args.only_steps:
+        sim.close()
+        if rank == 0:
+            print(json.dumps({"only_steps": True, "ms_per_step": ms / args.steps, "form": args.precision}))
+        return None
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.barrier()
@@ -363,7 +370,7 @@ def main():
             dist.destroy_process_group()
         return
     out = run_ours(args, rank, world, local)
-    if rank == 0:
+    if rank == 0 and out is not None:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(workload(args.n), args)
         print(json.dumps(out))
