@@ -72,6 +72,7 @@ SIGNATURES = {
     "sph_step_async": (C.c_int32, [_H, C.c_int64, C.c_int64]),
     "sph_synchronize": (C.c_int32, [_H]),
     "sph_download_fluid": (C.c_int32, [_H, C.c_int64, C.POINTER(C.c_int64)] + [_DP] * 10),
+    "sph_download_ids": (C.c_int32, [_H, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_stats": (C.c_int32, [_H, C.POINTER(SphStats)]),
     "sph_count_pairs": (C.c_int32, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_get_stream": (C.c_int32, [_H, C.POINTER(C.c_void_p)]),

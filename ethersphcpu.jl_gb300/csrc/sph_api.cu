@@ -713,6 +713,25 @@ int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, doubl
     return SPH_OK;
 }
 
+int32_t sph_download_ids(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* ids_out) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!n_out) return fail(h, SPH_ERR_ARG, "n_out is required");
+    cudaStream_t st = h->stream;
+    int32_t n32 = 0;
+    SPH_CUDA(h, cudaMemcpyAsync(&n32, h->nbuf + h->par, 4, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    const int64_t n = h->have_fluid ? n32 : 0;
+    *n_out = n;
+    if (n > capacity) return fail(h, SPH_ERR_ARG, "caller array too small for the live fluid");
+    if (n == 0 || !ids_out) return SPH_OK;
+    std::vector<int32_t> ids(n);
+    SPH_CUDA(h, cudaMemcpyAsync(ids.data(), h->S[h->par].id, n * 4, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    std::sort(ids.begin(), ids.end());
+    for (int64_t k = 0; k < n; ++k) ids_out[k] = ids[k];
+    return SPH_OK;
+}
+
 int32_t sph_stats(SphHandle* h, SphStats* out) {
     if (!h || !out) return fail(h, SPH_ERR_ARG, "null argument");
     std::memset(out, 0, sizeof(*out));

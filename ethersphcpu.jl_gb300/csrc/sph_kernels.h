@@ -46,3 +46,4 @@ void launch_count_pairs(const LaunchCtx& L, unsigned long long* d_counts);
 int scan_max_cells();
 
 }  // namespace sph
+

@@ -160,6 +160,14 @@ class Simulation:
         if self.thermal:
             fluid.t_[:] = r["t"]
 
+    def download_ids(self) -> np.ndarray:
+        """Original indices (of the last upload) of the live particles, ascending."""
+        cap = self.stats().n_fluid
+        ids = np.zeros(max(cap, 1), dtype=np.int64)
+        n = C.c_int64()
+        self._check(self.lib.sph_download_ids(self.h, cap, C.byref(n), ids.ctypes.data_as(C.POINTER(C.c_int64))))
+        return ids[: n.value]
+
     def stats(self) -> _abi.SphStats:
         s = _abi.SphStats()
         self._check(self.lib.sph_stats(self.h, C.byref(s)))

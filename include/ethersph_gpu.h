@@ -197,6 +197,11 @@ int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, doubl
                            double* v, double* rho, double* p, double* c, double* mass,
                            double* gap, double* t, double* kappa, double* cp);
 
+/* Indices (0-based, into the arrays of the last sph_upload_fluid) of the live fluid
+ * particles, ascending: the positions deleteat! would have kept.  Same order as
+ * sph_download_fluid. */
+int32_t sph_download_ids(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* ids);
+
 /* FP64 reductions over the live fluid (mass, kinetic energy, max speed). */
 int32_t sph_stats(SphHandle* h, SphStats* out);
 

@@ -221,3 +221,18 @@ def test_solve_entry_point(pkg, orc):
               domain_hi=s.domain_hi)
     got = dict(x=s.fluid.x_vec_, v=s.fluid.v_vec_, rho=s.fluid.rho_)
     compare(got, ref, 1e-12, keys=("x", "v", "rho"))
+
+
+def test_download_ids_name_the_survivors(pkg, orc):
+    s = scenes_mod().dam_break_2d(dx=0.04)
+    s.check = pkg.AABBCheck(hi=(4.0, 1.0))
+    with pkg.Simulation(s.params(), s.n_fluid, s.n_wall) as sim:
+        for w in s.walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(s.fluid)
+        sim.step(1, 12)
+        ids = sim.download_ids()
+        got = sim.download()
+    assert len(ids) == len(got["rho"]) < s.n_fluid
+    assert np.all(np.diff(ids) > 0)
+    assert np.array_equal(got["mass"], s.fluid.mass_[ids])
