@@ -77,6 +77,8 @@ SIGNATURES = {
     "sph_count_pairs": (C.c_int32, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_get_stream": (C.c_int32, [_H, C.POINTER(C.c_void_p)]),
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
+    "sph_count_pairs_noalloc": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]),
     "sph_last_error": (C.c_char_p, [_H]),
     "sph_destroy": (C.c_int32, [_H]),
 }

@@ -184,6 +184,12 @@ int32_t host_cell_key(const SceneDev& S, int dim, const double* x) {
 
 }  // namespace
 
+namespace sph {
+// Shared with entry points defined in other translation units.
+bool scene_from_params(const SphParams& p, SceneDev& S, std::string& err) { return build_scene(p, S, err); }
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace sph
+
 struct SphHandle {
     SphParams prm{};
     SceneDev scene{};

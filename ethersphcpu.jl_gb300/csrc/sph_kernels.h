@@ -47,3 +47,11 @@ int scan_max_cells();
 
 }  // namespace sph
 
+#include <string>
+
+namespace sph {
+// Parameter block -> scene constants (defined in sph_api.cu).
+bool scene_from_params(const SphParams& p, SceneDev& S, std::string& err);
+// Text returned by sph_last_error(NULL).
+void set_global_error(const std::string& msg);
+}  // namespace sph

@@ -226,6 +226,24 @@ enum {
 };
 int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out);
 
+/* Pair counting that allocates no device memory.  No counterpart in the reference:
+ * it serves callers that cannot let a library call cudaMalloc or cudaFree (device
+ * memory owned by another framework's stream-ordered pool, code that must not cause
+ * the device-wide synchronisation cudaMalloc/cudaFree can trigger).
+ * Counts the same pairs as sph_count_pairs for particles the caller holds in DEVICE
+ * memory: x (dim x n packed), wall_x (dim x n_wall packed); writes
+ * counts[0] = unique fluid pairs, counts[1] = fluid-wall pairs into the caller's device
+ * array counts[2].  Work is enqueued on `stream` (a cudaStream_t; NULL = legacy default
+ * stream) and the call returns without waiting.
+ * The cell list lives in one static device array of the library (about 10 MB, resident
+ * on every GPU that loaded the library until the process exits): at most 262,144 fluid
+ * and 262,144 wall particles and 262,144 grid cells; larger inputs return SPH_ERR_ARG.
+ * The first call on a device looks up that array's device address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU race, so
+ * serialise them on one stream.  Errors: sph_last_error(NULL). */
+int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double* x, int64_t n_wall,
+                                const double* wall_x, int64_t* counts, void* stream);
+
 /* Text of the last error on this handle (or of the last failed sph_create when h is NULL). */
 const char* sph_last_error(const SphHandle* h);
 
