@@ -176,6 +176,16 @@ def algorithmic_bytes(scene, precision):
     return nf * fluid + nw * wall
 
 
+def grid_cells(scene):
+    """Cells of the scene's grid (edge r_cut (1 + 1e-9), as the library builds it)."""
+    import math
+    edge = scene.kernel.influence_radius_ * (1.0 + 1e-9)
+    n = 1
+    for a in range(scene.kernel.dim_):
+        n *= max(1, math.ceil((scene.domain_hi[a] - scene.domain_lo[a]) / edge))
+    return n
+
+
 def time_form(pkg, _abi, scene, precision, steps, warmup, local):
     """Plain device timing of one form (CUDA events around each step, L2 flushed)."""
     import torch
@@ -220,6 +230,7 @@ def run_ours(args, rank, world, local):
     for w in scene.walls:
         sim.upload_walls(w)
     sim.upload_fluid(scene.fluid)
+    launch_shape = sim.autotune(3)  # lanes per particle x block size, picked on this scene
     lib, h = sim.lib, sim.h
     stream = torch.cuda.ExternalStream(sim.stream())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -332,7 +343,11 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": d2h / e2e_steps,
                 "what": f"upload + {e2e_steps} steps + download per iteration, {e2e_iters} iterations"},
         "plain_fp64": other,
-        "gpu_launches": args.steps * 7 + reinit_steps,
+        "launch_shape": {"continuity_lanes": launch_shape[0], "momentum_lanes": launch_shape[1],
+                         "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": "sph_autotune"},
+        # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, else 3), fill,
+        # placement; plus the Shepard kernel on re-initialisation steps
+        "gpu_launches": args.steps * (4 + (1 if grid_cells(scene) <= 16384 else 3)) + reinit_steps,
         "clocks": clocks,
     }
     return out

@@ -79,6 +79,8 @@ SIGNATURES = {
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
     "sph_count_pairs_noalloc": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
                                             C.c_void_p, C.c_void_p]),
+    "sph_autotune": (C.c_int32, [_H, C.c_int32, C.POINTER(C.c_int32)]),
+    "sph_set_launch_shape": (C.c_int32, [_H, C.POINTER(C.c_int32)]),
     "sph_last_error": (C.c_char_p, [_H]),
     "sph_destroy": (C.c_int32, [_H]),
 }

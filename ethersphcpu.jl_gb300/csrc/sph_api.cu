@@ -210,6 +210,8 @@ struct SphHandle {
     int64_t* h_pinned_step = nullptr;
     int par = 0;
     int64_t dev_step = INT64_MIN;  // value of the device step counter (host mirror)
+    // FP32 launch shape: lanes per particle for continuity, momentum, Shepard; block size
+    int tune[4] = {4, 4, 4, 128};
     bool have_fluid = false;
     int64_t steps_done = 0;
     std::string err;
@@ -276,6 +278,7 @@ cudaError_t alloc_sorted(SphHandle* h, SortedState& s) {
         if ((e = dalloc(h, &s.fc, n)) != cudaSuccess) return e;
         if ((e = dalloc(h, &s.fd, n)) != cudaSuccess) return e;
         if ((e = dalloc(h, &s.cell, n)) != cudaSuccess) return e;
+        if ((e = dalloc(h, &s.vol, n)) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
@@ -300,6 +303,10 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.sc.n_live = h->nbuf + h->par;
     L.n_next = h->nbuf + (h->par ^ 1);
     L.force_reinit = 0;
+    L.block = h->tune[3];
+    L.tpp_continuity = h->tune[0];
+    L.tpp_momentum = h->tune[1];
+    L.tpp_reinit = h->tune[2];
     return L;
 }
 
@@ -312,7 +319,7 @@ void launch_physics(int stage, const LaunchCtx& L) {
 // decision for the step (the kernel re-checks it per scene).
 void enqueue_step(SphHandle* h, bool reinit) {
     LaunchCtx L = make_ctx(h);
-    cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, h->stream);
+    // count[] was zeroed by the previous placement (or by the upload)
     launch_physics(0, L);
     launch_physics(1, L);
     if (reinit) launch_physics(2, L);
@@ -826,6 +833,8 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
             launch_hash(Lh);
         }
     }
+    // the momentum stage left arrivals in count[]: the next step expects it zeroed
+    SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
     // restore p and c (output-only fields) from the copy the placement stage wrote
     const size_t n = (size_t)h->cap;
     SPH_CUDA(h, cudaMemcpyAsync(h->S[par].p, h->S[par ^ 1].p, n * 8, cudaMemcpyDeviceToDevice, st));
@@ -834,6 +843,81 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
     SPH_CUDA(h, cudaStreamSynchronize(st));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    return SPH_OK;
+}
+
+int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
+    if (!h || reps < 1) return fail(h, SPH_ERR_ARG, "bad argument");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
+    if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
+        cudaStream_t st = h->stream;
+        cudaEvent_t e0, e1;
+        SPH_CUDA(h, cudaEventCreate(&e0));
+        SPH_CUDA(h, cudaEventCreate(&e1));
+        const int par = h->par;
+        const size_t nbytes = (size_t)h->cap * 8;
+        // p and c are output fields of the last step; the timed continuity launches
+        // overwrite them, so park them in the idle sorted buffer meanwhile
+        SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].p, h->S[par].p, nbytes, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].c, h->S[par].c, nbytes, cudaMemcpyDeviceToDevice, st));
+        const int tpps[4] = {1, 2, 4, 8};
+        const int blocks[3] = {64, 128, 256};
+        int best_tpp[3] = {4, 4, 4};
+        int best_block[3] = {128, 128, 128};
+        for (int stage = 0; stage < 3; ++stage) {
+            float best = 1e30f;
+            for (int tpp : tpps)
+                for (int block : blocks) {
+                    LaunchCtx L = make_ctx(h);
+                    L.force_reinit = 1;
+                    L.block = block;
+                    L.tpp_continuity = L.tpp_momentum = L.tpp_reinit = tpp;
+                    launch_physics(stage, L);  // warm-up
+                    SPH_CUDA(h, cudaEventRecord(e0, st));
+                    for (int r = 0; r < reps; ++r) launch_physics(stage, L);
+                    SPH_CUDA(h, cudaEventRecord(e1, st));
+                    SPH_CUDA(h, cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    SPH_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) {
+                        best = ms;
+                        best_tpp[stage] = tpp;
+                        best_block[stage] = block;
+                    }
+                }
+        }
+        // one block size for all three stages: the momentum stage's (it dominates)
+        h->tune[0] = best_tpp[0];
+        h->tune[1] = best_tpp[1];
+        h->tune[2] = best_tpp[2];
+        h->tune[3] = best_block[1];
+        // restore what the timed launches touched: p and c, and the arrivals left in
+        // count[]; every other field they wrote is rebuilt by the next step before use
+        SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->S[par].p, h->S[par ^ 1].p, nbytes, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->S[par].c, h->S[par ^ 1].c, nbytes, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaGetLastError());
+        SPH_CUDA(h, cudaStreamSynchronize(st));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+        h->graphs.clear();
+    }
+    if (out)
+        for (int k = 0; k < 4; ++k) out[k] = h->tune[k];
+    return SPH_OK;
+}
+
+int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
+    if (!h || !shape) return fail(h, SPH_ERR_ARG, "null argument");
+    for (int k = 0; k < 3; ++k)
+        if (shape[k] != 1 && shape[k] != 2 && shape[k] != 4 && shape[k] != 8)
+            return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4 or 8");
+    if (shape[3] < 32 || shape[3] > 1024 || shape[3] % 32 != 0)
+        return fail(h, SPH_ERR_ARG, "block size must be a multiple of 32 in [32, 1024]");
+    for (int k = 0; k < 4; ++k) h->tune[k] = shape[k];
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
     return SPH_OK;
 }
 

@@ -106,6 +106,7 @@ struct SortedState {
     float4* fc;   // 2D: (T, kappa, cp, -)     3D: (P, gap, T, kappa)
     float* fd;    // 3D: cp
     int32_t* cell;  // cell key of the particle (global)
+    double* vol;    // m / rho after continuity (FP32 form: FP64 Shepard weights)
 };
 
 struct NextState {

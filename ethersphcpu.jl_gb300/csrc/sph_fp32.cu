@@ -1,17 +1,25 @@
-// sph_fp32.cu — FP32-compensated form of the continuity and momentum gathers.
+// sph_fp32.cu — FP32-compensated form of the continuity, momentum and Shepard gathers.
 //
 // Pair arithmetic runs in FP32 on cell-relative positions: every particle carries
 // (x - origin of its cell) as floats, and a neighbour in the cell offset (dx, dy, dz)
 // sits at xr_j + (dx, dy, dz) * edge in the frame of particle i's cell, so r_vec is
 // formed from numbers of magnitude <= 2 r_cut with an absolute error of a few 1e-9 r_cut.
-// The continuity and force sums are Kahan-compensated FP32 accumulators; the result
-// (sum - compensation) is taken to FP64 before the forward-Euler update, which runs in
-// FP64 on the FP64 master position / velocity / density / temperature.  The Shepard
-// re-initialisation keeps its FP64 kernel (sph_fp64.cu).
+// Continuity and force sums are Kahan-compensated FP32 accumulators; the result
+// (sum - compensation) goes to FP64 before the forward-Euler update, which runs in FP64
+// on the FP64 master position / velocity / density / temperature.  The Shepard sums
+// accumulate in FP64 (FP32 kernel values times FP64 volumes and masses).
+//
+// Each particle's neighbour walk is split over TPP consecutive lanes of a warp: lane t
+// takes candidates t, t+TPP, ... of every neighbour row (the three x-cells of a row are
+// one virtual range), keeps its own compensated partial sums, and the lanes combine
+// them with an xor butterfly in FP64 — every lane ends with the bitwise same total, so
+// results are deterministic for a given TPP.  TPP and the block size are launch
+// parameters picked by the autotuner (more lanes per particle = more warps in flight to
+// hide the dependent neighbour loads).
 //
 // Same terms, order of walls after fluid, and solve variants as sph_fp64.cu; the
 // formulas follow Continuity.jl, PressureForce.jl, ViscosityForce.jl, WallForce.jl,
-// ThermalConduction.jl and SelfAction/*.jl.
+// ThermalConduction.jl, SelfAction/*.jl and ReconstructValue.jl.
 #include "sph_physics.cuh"
 #include "sph_kernels.h"
 
@@ -31,6 +39,20 @@ struct Kahan {
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+
+template <int TPP>
+__device__ __forceinline__ unsigned group_mask() {
+    if (TPP == 32) return 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    return ((1u << TPP) - 1u) << (lane & ~(unsigned)(TPP - 1));
+}
+
+template <int TPP>
+__device__ __forceinline__ double group_sum(double v, unsigned mask) {
+#pragma unroll
+    for (int o = TPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    return v;
+}
 
 // W and dW/dr in FP32 (same polynomials as sph_physics.cuh).
 template <int KK>
@@ -87,11 +109,12 @@ __device__ __forceinline__ float kernel_w_f(float q, const SceneDev& S) {
     return W;
 }
 
-// Visits the neighbour cells one by one (z, y, x order), handing the callback the
-// cell's sorted range and its offset from particle i's cell in metres.
-template <int DIM, typename F>
-__device__ __forceinline__ void walk_cells_rel(const SceneDev& S, const int32_t* __restrict__ start,
-                                               const int32_t c[3], F&& f) {
+// Neighbour rows in (z, y) order; inside a row the cells x-1, x, x+1 (wrapping on a
+// periodic axis, skipped off the grid) form one virtual range that the TPP lanes share.
+// The callback gets the sorted index j and the offset of j's cell from i's cell (m).
+template <int DIM, int TPP, typename F>
+__device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
+                                           int lane, F&& f) {
     const int zr = DIM == 3 ? 1 : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
         const int z = c[2] + dz;
@@ -100,77 +123,89 @@ __device__ __forceinline__ void walk_cells_rel(const SceneDev& S, const int32_t*
             const int y = c[1] + dy;
             if (y < 0 || y >= S.n[1]) continue;
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
-            for (int dx = -1; dx <= 1; ++dx) {
-                int x = c[0] + dx;
+            const float oy = (float)dy * S.cell_f[1];
+            const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
+            // the row's cells are one virtual range v = 0 .. len0+len1+len2-1; lane t
+            // takes v = t, t+TPP, ...  Each cell is walked in turn from the first v of
+            // the lane inside it (unrolled: every index stays in a register).
+            int prefix = 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                int x = c[0] + k - 1;
+                bool ok = true;
                 if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
-                else if (x < 0 || x >= S.n[0]) continue;
-                const float ox = (float)dx * S.cell_f[0];
-                const float oy = (float)dy * S.cell_f[1];
-                const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
-                f(__ldg(start + row + x), __ldg(start + row + x + 1), ox, oy, oz);
+                else ok = x >= 0 && x < S.n[0];
+                if (!ok) continue;
+                const int b = __ldg(start + row + x);
+                const int e = __ldg(start + row + x + 1);
+                const float ox = (float)(k - 1) * S.cell_f[0];
+                const int first = (lane - prefix) & (TPP - 1);
+                for (int j = b + first; j < e; j += TPP) f(j, ox, oy, oz);
+                prefix += e - b;
             }
         }
     }
 }
 
+__device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int32_t c[3]) {
+    const int32_t k = key - S.cell_off;
+    c[0] = k % S.n[0];
+    c[1] = (k / S.n[0]) % S.n[1];
+    c[2] = k / (S.n[0] * S.n[1]);
+}
+
 // -------------------------------------------------------------------- K4 (FP32)
-template <int DIM, int KK>
-__global__ void __launch_bounds__(128) k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st,
-                                                        const int32_t* __restrict__ start,
-                                                        const int32_t* __restrict__ n_live, int32_t cap) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <int DIM, int KK, int TPP>
+__global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st,
+                                 const int32_t* __restrict__ start, const int32_t* __restrict__ n_live, int32_t cap) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *n_live) return;
     const SceneDev& S = scenes[st.scene[i]];
     const float4 ai = st.fa[i];
-    const float4 bi = st.fb[i];
     float xi[3], vi[3];
     if (DIM == 2) {
         xi[0] = ai.x; xi[1] = ai.y; xi[2] = 0.f;
         vi[0] = ai.z; vi[1] = ai.w; vi[2] = 0.f;
     } else {
+        const float4 bi = st.fb[i];
         xi[0] = ai.x; xi[1] = ai.y; xi[2] = ai.z;
         vi[0] = bi.x; vi[1] = bi.y; vi[2] = bi.z;
     }
     int32_t c[3];
-    {
-        const int32_t key = st.cell[i] - S.cell_off;
-        c[0] = key % S.n[0];
-        c[1] = (key / S.n[0]) % S.n[1];
-        c[2] = key / (S.n[0] * S.n[1]);
-    }
+    decode_cell(st.cell[i], S, c);
     Kahan drho;
-    walk_cells_rel<DIM>(S, start, c, [&](int jb, int je, float ox, float oy, float oz) {
-        const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
-        for (int j = jb; j < je; ++j) {
-            if (j == i) continue;
-            const float4 aj = st.fa[j];
-            const float rx = bx - aj.x, ry = by - aj.y;
-            const float rz = DIM == 3 ? bz - aj.z : 0.f;
-            const float d2 = rx * rx + ry * ry + rz * rz;
-            if (!(d2 <= S.rc2_f) || d2 == 0.f) continue;
-            const float inv_r = rsqrtf(d2);
-            const float r = d2 * inv_r;
-            float W, dW;
-            kernel_wdw_f<KK>(r * S.inv_h_f, S, W, dW);
-            const float s = dW * inv_r;
-            float vx, vy, vz, mj;
-            if (DIM == 2) {
-                vx = vi[0] - aj.z;
-                vy = vi[1] - aj.w;
-                vz = 0.f;
-                mj = st.fb[j].x;
-            } else {
-                const float4 bj = st.fb[j];
-                vx = vi[0] - bj.x;
-                vy = vi[1] - bj.y;
-                vz = vi[2] - bj.z;
-                mj = aj.w;
-            }
-            drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
+    walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz) {
+        if (j == i) return;
+        const float4 aj = st.fa[j];
+        const float4 bj = st.fb[j];  // loaded with aj: one round trip per candidate
+        const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
+        const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
+        const float d2 = rx * rx + ry * ry + rz * rz;
+        if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
+        const float inv_r = rsqrtf(d2);
+        const float r = d2 * inv_r;
+        float W, dW;
+        kernel_wdw_f<KK>(r * S.inv_h_f, S, W, dW);
+        const float s = dW * inv_r;
+        float vx, vy, vz, mj;
+        if (DIM == 2) {
+            vx = vi[0] - aj.z;
+            vy = vi[1] - aj.w;
+            vz = 0.f;
+            mj = bj.x;
+        } else {
+            vx = vi[0] - bj.x;
+            vy = vi[1] - bj.y;
+            vz = vi[2] - bj.z;
+            mj = aj.w;
         }
+        drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
     });
+    const double dr = group_sum<TPP>(drho.value(), group_mask<TPP>());
+    if (lane != 0) return;
     double rho = st.rho[i];
-    rho += drho.value() * S.dt;
+    rho += dr * S.dt;
     const double rr = rho / S.rho0;
     const double p = S.b * (jl_powi(rr, S.gamma) - 1.0) + S.p0;
     const double cs = S.c0 * sqrt(jl_powi(rr, S.gamma - 1));
@@ -179,9 +214,12 @@ __global__ void __launch_bounds__(128) k_continuity_f32(const SceneDev* __restri
     st.p[i] = p;
     st.c[i] = cs;
     st.P[i] = P;
+    st.vol[i] = st.m[i] / rho;
     if (DIM == 2) {
+        const float4 bi = st.fb[i];
         st.fb[i] = make_float4(bi.x, (float)rho, (float)P, bi.w);
     } else {
+        const float4 bi = st.fb[i];
         st.fb[i] = make_float4(bi.x, bi.y, bi.z, (float)rho);
         const float4 ci = st.fc[i];
         st.fc[i] = make_float4((float)P, ci.y, ci.z, ci.w);
@@ -189,15 +227,15 @@ __global__ void __launch_bounds__(128) k_continuity_f32(const SceneDev* __restri
 }
 
 // -------------------------------------------------------------------- K5 (FP32)
-template <int DIM, int KK, int MODE>
-__global__ void __launch_bounds__(128) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st,
-                                                      NextState nx, WallState wl, SortScratch sc, int32_t cap) {
+template <int DIM, int KK, int MODE, int TPP>
+__global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
+                               SortScratch sc, int32_t cap) {
     using V = typename VecT<DIM>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
-    const int64_t step = sc.scene_step[s];
     const float4 ai = st.fa[i];
     const float4 bi = st.fb[i];
     float xi[3], vi[3], m_i, rho_i, P_i, gap_i;
@@ -225,156 +263,151 @@ __global__ void __launch_bounds__(128) k_momentum_f32(const SceneDev* __restrict
     const float inv_Wg_i = 1.f / kernel_w_f<KK>(gap_i * inv_h, S);
     const float inv_cp_i = 1.f / cp_i;
     int32_t c[3];
-    {
-        const int32_t key = st.cell[i] - S.cell_off;
-        c[0] = key % S.n[0];
-        c[1] = (key / S.n[0]) % S.n[1];
-        c[2] = key / (S.n[0] * S.n[1]);
-    }
+    decode_cell(st.cell[i], S, c);
     Kahan dv[3], dT;
 
-    walk_cells_rel<DIM>(S, sc.start, c, [&](int jb, int je, float ox, float oy, float oz) {
-        const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
-        for (int j = jb; j < je; ++j) {
-            if (j == i) continue;
-            const float4 aj = st.fa[j];
-            const float rx = bx - aj.x, ry = by - aj.y;
-            const float rz = DIM == 3 ? bz - aj.z : 0.f;
-            const float d2 = rx * rx + ry * ry + rz * rz;
-            if (!(d2 <= S.rc2_f) || d2 == 0.f) continue;
-            const float inv_r = rsqrtf(d2);
-            const float r = d2 * inv_r;
-            float W, dW;
-            kernel_wdw_f<KK>(r * inv_h, S, W, dW);
-            const float4 bj = st.fb[j];
-            float vx, vy, vz, m_j, rho_j, P_j, gap_j;
-            float T_j = 0.f, kap_j = 0.f;
-            if (DIM == 2) {
-                vx = vi[0] - aj.z; vy = vi[1] - aj.w; vz = 0.f;
-                m_j = bj.x; rho_j = bj.y; P_j = bj.z; gap_j = bj.w;
-                if (MODE == kModeThermal) {
-                    const float4 cj = st.fc[j];
-                    T_j = cj.x; kap_j = cj.y;
-                }
-            } else {
-                vx = vi[0] - bj.x; vy = vi[1] - bj.y; vz = vi[2] - bj.z;
-                m_j = aj.w; rho_j = bj.w;
-                const float4 cj = st.fc[j];
-                P_j = cj.x; gap_j = cj.y;
-                if (MODE == kModeThermal) {
-                    T_j = cj.z; kap_j = cj.w;
-                }
+    walk_lanes<DIM, TPP>(S, sc.start, c, lane, [&](int j, float ox, float oy, float oz) {
+        if (j == i) return;
+        // issue every load of the candidate before the distance test: one memory
+        // round trip per candidate instead of two for the accepted ones
+        const float4 aj = st.fa[j];
+        const float4 bj = st.fb[j];
+        float4 cj = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (DIM == 3 || MODE == kModeThermal) cj = st.fc[j];
+        const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
+        const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
+        const float d2 = rx * rx + ry * ry + rz * rz;
+        if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
+        const float inv_r = rsqrtf(d2);
+        const float r = d2 * inv_r;
+        float W, dW;
+        kernel_wdw_f<KK>(r * inv_h, S, W, dW);
+        float vx, vy, vz, m_j, rho_j, P_j, gap_j;
+        float T_j = 0.f, kap_j = 0.f;
+        if (DIM == 2) {
+            vx = vi[0] - aj.z; vy = vi[1] - aj.w; vz = 0.f;
+            m_j = bj.x; rho_j = bj.y; P_j = bj.z; gap_j = bj.w;
+            if (MODE == kModeThermal) {
+                T_j = cj.x; kap_j = cj.y;
             }
-            // pressure (PressureForce.jl:14-19), tensile term included
-            float prho2 = P_i + P_j;
-            const float inv_Wg = S.uniform_gap ? inv_Wg_i : 1.f / kernel_w_f<KK>(0.5f * (gap_i + gap_j) * inv_h, S);
-            prho2 += fabsf(prho2) * 0.01f * W * inv_Wg;
-            // viscosity (ViscosityForce.jl:15-23)
-            const float sum_rho = rho_i + rho_j;
-            const float f = 4.f * (mu_i + S.nu0_f * rho_j) * r * dW / (sum_rho * sum_rho * (r * r + S.hh001_f));
-            const float gp = -m_j * prho2 * dW * inv_r;  // pressure term along r_vec
-            const float gv = m_j * f;                    // viscosity term along v_ij
-            dv[0].add(gp * rx + gv * vx);
-            dv[1].add(gp * ry + gv * vy);
-            if (DIM == 3) dv[2].add(gp * rz + gv * vz);
-            if (MODE == kModeThermal) {  // ThermalConduction.jl:15-21
-                const float keq = 2.f * kap_i * kap_j / (kap_i + kap_j);
-                const float dq = 2.f * keq * r * dW / (rho_i * rho_j * (r * r + S.hh001_f)) * (T_i - T_j);
-                dT.add(dq * m_j * inv_cp_i);
+        } else {
+            vx = vi[0] - bj.x; vy = vi[1] - bj.y; vz = vi[2] - bj.z;
+            m_j = aj.w; rho_j = bj.w;
+            P_j = cj.x; gap_j = cj.y;
+            if (MODE == kModeThermal) {
+                T_j = cj.z; kap_j = cj.w;
             }
+        }
+        // pressure (PressureForce.jl:14-19), tensile term included
+        float prho2 = P_i + P_j;
+        const float inv_Wg = S.uniform_gap ? inv_Wg_i : 1.f / kernel_w_f<KK>(0.5f * (gap_i + gap_j) * inv_h, S);
+        prho2 += fabsf(prho2) * 0.01f * W * inv_Wg;
+        // viscosity (ViscosityForce.jl:15-23)
+        const float sum_rho = rho_i + rho_j;
+        const float f = __fdividef(4.f * (mu_i + S.nu0_f * rho_j) * r * dW, sum_rho * sum_rho * (r * r + S.hh001_f));
+        const float gp = -m_j * prho2 * dW * inv_r;  // pressure term along r_vec
+        const float gv = m_j * f;                    // viscosity term along v_ij
+        dv[0].add(gp * rx + gv * vx);
+        dv[1].add(gp * ry + gv * vy);
+        if (DIM == 3) dv[2].add(gp * rz + gv * vz);
+        if (MODE == kModeThermal) {  // ThermalConduction.jl:15-21
+            const float keq = __fdividef(2.f * kap_i * kap_j, kap_i + kap_j);
+            const float dq = __fdividef(2.f * keq * r * dW, rho_i * rho_j * (r * r + S.hh001_f)) * (T_i - T_j);
+            dT.add(dq * m_j * inv_cp_i);
         }
     });
 
     if (wl.n > 0) {
-        walk_cells_rel<DIM>(S, wl.start, c, [&](int jb, int je, float ox, float oy, float oz) {
-            const float bx = xi[0] - ox, by = xi[1] - oy, bz = xi[2] - oz;
-            for (int w = jb; w < je; ++w) {
-                const float4 wa = wl.fa[w];
-                const float4 wb = wl.fb[w];
-                float rv[3], n[3], vv[3], gw, Tw = 0.f, kw = 0.f;
-                bool thermo = false;
-                if (DIM == 2) {
-                    rv[0] = bx - wa.x; rv[1] = by - wa.y; rv[2] = 0.f;
-                    n[0] = wa.z; n[1] = wa.w; n[2] = 0.f;
-                    vv[0] = vi[0] - wb.x; vv[1] = vi[1] - wb.y; vv[2] = 0.f;
-                    gw = wb.z;
-                    if (MODE == kModeThermal) {
-                        const float4 wc = wl.fc[w];
-                        Tw = wb.w; kw = wc.x; thermo = wc.y != 0.f;
-                    }
-                } else {
-                    rv[0] = bx - wa.x; rv[1] = by - wa.y; rv[2] = bz - wa.z;
-                    gw = wa.w;
-                    n[0] = wb.x; n[1] = wb.y; n[2] = wb.z;
+        walk_lanes<DIM, TPP>(S, wl.start, c, lane, [&](int w, float ox, float oy, float oz) {
+            const float4 wa = wl.fa[w];
+            const float4 wb = wl.fb[w];
+            float rv[3], n[3], vv[3], gw, Tw = 0.f, kw = 0.f;
+            bool thermo = false;
+            if (DIM == 2) {
+                rv[0] = xi[0] - ox - wa.x; rv[1] = xi[1] - oy - wa.y; rv[2] = 0.f;
+                n[0] = wa.z; n[1] = wa.w; n[2] = 0.f;
+                vv[0] = vi[0] - wb.x; vv[1] = vi[1] - wb.y; vv[2] = 0.f;
+                gw = wb.z;
+                if (MODE == kModeThermal) {
                     const float4 wc = wl.fc[w];
-                    vv[0] = vi[0] - wc.x; vv[1] = vi[1] - wc.y; vv[2] = vi[2] - wc.z;
-                    if (MODE == kModeThermal) {
-                        Tw = wb.w; kw = wc.w; thermo = wl.kind[w] == SPH_WALL_THERMOSTATIC;
-                    }
+                    Tw = wb.w; kw = wc.x; thermo = wc.y != 0.f;
                 }
-                const float d2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
-                if (!(d2 <= S.rc2_f)) continue;
-                const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
-                const float r = d2 * inv_r;
-                float W, dW;
-                kernel_wdw_f<KK>(r * inv_h, S, W, dW);
-                const float vert = vv[0] * n[0] + vv[1] * n[1] + vv[2] * n[2];
-                float acc[3] = {0.f, 0.f, 0.f};
-                {  // WallForce.jl:15-28
-                    const float psi = fabsf(rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2]);
-                    const float xi_ = sqrtf(fmaxf(r * r - psi * psi, 0.f));
-                    const float q = psi / gw;
-                    if (!(q > 1.f || xi_ > gw)) {
-                        const float pxi = fabsf((1.f + cospif(xi_ / gw)) * 0.5f);
-                        const float beta = vert > 0.f ? 0.f : 1.f;
-                        const float rpsi = (0.01f * c_i * c_i + beta * c_i * fabsf(vert)) * inv_h * fabsf(1.f - q) *
-                                           rsqrtf(q);
-                        const float wf = rpsi * pxi;
-                        acc[0] += wf * n[0];
-                        acc[1] += wf * n[1];
-                        acc[2] += wf * n[2];
-                    }
+            } else {
+                rv[0] = xi[0] - ox - wa.x; rv[1] = xi[1] - oy - wa.y; rv[2] = xi[2] - oz - wa.z;
+                gw = wa.w;
+                n[0] = wb.x; n[1] = wb.y; n[2] = wb.z;
+                const float4 wc = wl.fc[w];
+                vv[0] = vi[0] - wc.x; vv[1] = vi[1] - wc.y; vv[2] = vi[2] - wc.z;
+                if (MODE == kModeThermal) {
+                    Tw = wb.w; kw = wc.w; thermo = wl.kind[w] == SPH_WALL_THERMOSTATIC;
                 }
-                if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
-                    float prho2 = P_i + S.P_bg_f;
-                    prho2 += fabsf(prho2) * 0.01f * W * inv_Wg_i;
-                    const float gp = -m_i * prho2 * dW * inv_r;
-                    acc[0] += gp * rv[0];
-                    acc[1] += gp * rv[1];
-                    acc[2] += gp * rv[2];
+            }
+            const float d2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+            if (!(d2 <= S.rc2_f)) return;
+            const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
+            const float r = d2 * inv_r;
+            float W, dW;
+            kernel_wdw_f<KK>(r * inv_h, S, W, dW);
+            const float vert = vv[0] * n[0] + vv[1] * n[1] + vv[2] * n[2];
+            float acc[3] = {0.f, 0.f, 0.f};
+            {  // WallForce.jl:15-28
+                const float psi = fabsf(rv[0] * n[0] + rv[1] * n[1] + rv[2] * n[2]);
+                const float xi_ = sqrtf(fmaxf(r * r - psi * psi, 0.f));
+                const float q = psi / gw;
+                if (!(q > 1.f || xi_ > gw)) {
+                    const float pxi = fabsf((1.f + cospif(xi_ / gw)) * 0.5f);
+                    const float beta = vert > 0.f ? 0.f : 1.f;
+                    const float rpsi =
+                        (0.01f * c_i * c_i + beta * c_i * fabsf(vert)) * inv_h * fabsf(1.f - q) * rsqrtf(q);
+                    const float wf = rpsi * pxi;
+                    acc[0] += wf * n[0];
+                    acc[1] += wf * n[1];
+                    acc[2] += wf * n[2];
                 }
-                {  // ViscosityForce.jl:34-44
-                    const float sum_rho = 2.f * rho_i;
-                    const float f = 8.f * mu_i * r * dW / (sum_rho * sum_rho * (r * r + S.hh001_f));
-                    const float gv = m_i * f;
-                    acc[0] += gv * (vv[0] - vert * n[0]);
-                    acc[1] += gv * (vv[1] - vert * n[1]);
-                    acc[2] += gv * (vv[2] - vert * n[2]);
-                }
-                dv[0].add(acc[0]);
-                dv[1].add(acc[1]);
-                if (DIM == 3) dv[2].add(acc[2]);
-                if (MODE == kModeThermal && thermo) {  // ThermalConduction.jl:31-35
-                    const float dq = S.inv_cp_f * (kap_i + kw) * r * dW * S.inv_rho0_f /
-                                     (rho_i * (r * r + S.hh001_f)) * (T_i - Tw);
-                    dT.add(dq * m_i);
-                }
+            }
+            if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
+                float prho2 = P_i + S.P_bg_f;
+                prho2 += fabsf(prho2) * 0.01f * W * inv_Wg_i;
+                const float gp = -m_i * prho2 * dW * inv_r;
+                acc[0] += gp * rv[0];
+                acc[1] += gp * rv[1];
+                acc[2] += gp * rv[2];
+            }
+            {  // ViscosityForce.jl:34-44
+                const float sum_rho = 2.f * rho_i;
+                const float f = __fdividef(8.f * mu_i * r * dW, sum_rho * sum_rho * (r * r + S.hh001_f));
+                const float gv = m_i * f;
+                acc[0] += gv * (vv[0] - vert * n[0]);
+                acc[1] += gv * (vv[1] - vert * n[1]);
+                acc[2] += gv * (vv[2] - vert * n[2]);
+            }
+            dv[0].add(acc[0]);
+            dv[1].add(acc[1]);
+            if (DIM == 3) dv[2].add(acc[2]);
+            if (MODE == kModeThermal && thermo) {  // ThermalConduction.jl:31-35
+                const float dq =
+                    __fdividef(S.inv_cp_f * (kap_i + kw) * r * dW * S.inv_rho0_f, rho_i * (r * r + S.hh001_f)) *
+                    (T_i - Tw);
+                dT.add(dq * m_i);
             }
         });
     }
 
-    // ---- FP64 forward Euler on the masters (UpdateTemperature/Velocity/Position.jl)
-    const V* __restrict__ xm = (const V*)st.x;
-    const V* __restrict__ vm = (const V*)st.v;
-    const V x0 = xm[i];
-    const V v0 = vm[i];
-    const double dt = S.dt;
+    const unsigned mask = group_mask<TPP>();
     double dvd[DIM];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) dvd[k] = dv[k].value();
+    for (int k = 0; k < DIM; ++k) dvd[k] = group_sum<TPP>(dv[k].value(), mask);
+    const double dTd = MODE == kModeThermal ? group_sum<TPP>(dT.value(), mask) : 0.0;
+    if (lane != 0) return;
+
+    // ---- FP64 forward Euler on the masters (UpdateTemperature/Velocity/Position.jl)
+    const int64_t step = sc.scene_step[s];
+    const V x0 = ((const V*)st.x)[i];
+    const V v0 = ((const V*)st.v)[i];
+    const double dt = S.dt;
     double body[DIM];
     if (MODE == kModeThermal) {
-        const double Tn = st.T[i] + dt * dT.value();
+        const double Tn = st.T[i] + dt * dTd;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) body[k] = S.bous[k] * (Tn - S.t0);
         nx.T[i] = Tn;
@@ -430,44 +463,88 @@ __global__ void __launch_bounds__(128) k_momentum_f32(const SceneDev* __restrict
     }
 }
 
-template <int DIM, int KK>
-void launch_k4(const LaunchCtx& L) {
-    const int grid = (L.cap + 127) / 128;
-    k_continuity_f32<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+// -------------------------------------------------------------------- K6 (FP32 W, FP64 sums)
+template <int DIM, int KK, int TPP>
+__global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, SortScratch sc,
+                             int32_t cap, int force) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / TPP, lane = t % TPP;
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    if (!force && !is_step(sc.scene_step[s], S.reinit_interval)) return;
+    const float4 ai = st.fa[i];
+    const float xi0 = ai.x, xi1 = ai.y, xi2 = DIM == 3 ? ai.z : 0.f;
+    int32_t c[3];
+    decode_cell(st.cell[i], S, c);
+    double sw = 0.0, sws = 0.0;
+    walk_lanes<DIM, TPP>(S, sc.start, c, lane, [&](int j, float ox, float oy, float oz) {
+        if (j == i) return;
+        const float4 aj = st.fa[j];
+        const float rx = xi0 - ox - aj.x, ry = xi1 - oy - aj.y;
+        const float rz = DIM == 3 ? xi2 - oz - aj.z : 0.f;
+        const float d2 = rx * rx + ry * ry + rz * rz;
+        if (!(d2 <= S.rc2_f)) return;
+        const double W = (double)kernel_w_f<KK>(sqrtf(d2) * S.inv_h_f, S);
+        sw += W * st.vol[j];
+        sws += W * st.m[j];
+    });
+    const unsigned mask = group_mask<TPP>();
+    sw = group_sum<TPP>(sw, mask);
+    sws = group_sum<TPP>(sws, mask);
+    if (lane != 0) return;
+    sw += S.k0 * st.vol[i];
+    sws += S.k0 * st.m[i];
+    nx.rho[i] = sws / sw;
 }
-template <int DIM, int KK, int MODE>
-void launch_k5(const LaunchCtx& L) {
-    const int grid = (L.cap + 127) / 128;
-    k_momentum_f32<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap);
+
+// -------------------------------------------------------------------- launchers
+template <int DIM, int KK, int TPP>
+void launch_tpp(int stage, int mode, const LaunchCtx& L) {
+    const int block = L.block > 0 ? L.block : 128;
+    const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
+    if (stage == 0) {
+        k_continuity_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+    } else if (stage == 2) {
+        k_reinit_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap, L.force_reinit);
+    } else if (mode == kModeFluidWall) {
+        k_momentum_f32<DIM, KK, kModeFluidWall, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc,
+                                                                                   L.cap);
+    } else if (mode == kModeWallPressure) {
+        k_momentum_f32<DIM, KK, kModeWallPressure, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
+                                                                                      L.sc, L.cap);
+    } else {
+        k_momentum_f32<DIM, KK, kModeThermal, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc,
+                                                                                 L.cap);
+    }
+}
+
+template <int DIM, int KK>
+void launch_kk(int stage, const LaunchCtx& L) {
+    const int tpp = stage == 0 ? L.tpp_continuity : (stage == 1 ? L.tpp_momentum : L.tpp_reinit);
+    switch (tpp) {
+        case 1: launch_tpp<DIM, KK, 1>(stage, L.mode, L); break;
+        case 2: launch_tpp<DIM, KK, 2>(stage, L.mode, L); break;
+        case 8: launch_tpp<DIM, KK, 8>(stage, L.mode, L); break;
+        default: launch_tpp<DIM, KK, 4>(stage, L.mode, L); break;
+    }
 }
 
 template <int DIM>
-void dispatch(int kk, int stage, int mode, const LaunchCtx& L) {
-#define SPH_KK_CASE(KKV)                                                              \
-    case KKV:                                                                         \
-        if (stage == 0) launch_k4<DIM, KKV>(L);                                       \
-        else if (mode == kModeFluidWall) launch_k5<DIM, KKV, kModeFluidWall>(L);      \
-        else if (mode == kModeWallPressure) launch_k5<DIM, KKV, kModeWallPressure>(L); \
-        else launch_k5<DIM, KKV, kModeThermal>(L);                                    \
-        break;
-    switch (kk) {
-        SPH_KK_CASE(SPH_KERNEL_CUBIC_SPLINE)
-        SPH_KK_CASE(SPH_KERNEL_GAUSSIAN)
-        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C2)
-        SPH_KK_CASE(SPH_KERNEL_WENDLAND_C4)
+void dispatch(int stage, const LaunchCtx& L) {
+    switch (L.kernel) {
+        case SPH_KERNEL_CUBIC_SPLINE: launch_kk<DIM, SPH_KERNEL_CUBIC_SPLINE>(stage, L); break;
+        case SPH_KERNEL_GAUSSIAN: launch_kk<DIM, SPH_KERNEL_GAUSSIAN>(stage, L); break;
+        case SPH_KERNEL_WENDLAND_C2: launch_kk<DIM, SPH_KERNEL_WENDLAND_C2>(stage, L); break;
+        default: launch_kk<DIM, SPH_KERNEL_WENDLAND_C4>(stage, L); break;
     }
-#undef SPH_KK_CASE
 }
 
 }  // namespace
 
 void launch_physics_fp32(int stage, const LaunchCtx& L) {
-    if (stage == 2) {  // Shepard sums stay FP64
-        launch_physics_fp64(2, L);
-        return;
-    }
-    if (L.dim == 2) dispatch<2>(L.kernel, stage, L.mode, L);
-    else dispatch<3>(L.kernel, stage, L.mode, L);
+    if (L.dim == 2) dispatch<2>(stage, L);
+    else dispatch<3>(stage, L);
 }
 
 }  // namespace sph

@@ -25,6 +25,9 @@ struct LaunchCtx {
     SortScratch sc;
     int32_t* n_next;  // live count after the sort being built
     int force_reinit; // 1: re-initialise every scene regardless of its step (stage timing)
+    // launch shape of the FP32 gathers (lanes per particle, threads per block)
+    int block;
+    int tpp_continuity, tpp_momentum, tpp_reinit;
 };
 
 // stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init

@@ -164,9 +164,11 @@ __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t c
 
 template <int DIM, bool THERMAL, bool SHADOW>
 __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, NextState nx, SortedState dst,
-                        SortScratch sc, int32_t cap) {
+                        SortScratch sc, int32_t cap, int32_t ncells) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // count[] has been scanned: clear it for the next step's arrivals
+    for (int k = i; k < ncells; k += gridDim.x * blockDim.x) sc.count[k] = 0;
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t key = sc.key[i];
     if (key == kDeadKey) return;
@@ -311,8 +313,44 @@ void launch_hash(const LaunchCtx& L) {
     else k_hash<3><<<grid, 128, 0, L.stream>>>(L.scenes, L.nx, L.st, L.sc, L.cap);
 }
 
+// Whole scan in one block when the grid has at most 1024 x 16 cells.
+__global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* __restrict__ count, int32_t n,
+                                                                int32_t* __restrict__ start,
+                                                                int32_t* __restrict__ n_next,
+                                                                int64_t* __restrict__ scene_step, int32_t nscenes,
+                                                                int advance) {
+    __shared__ int32_t warp_sums[kScanTopThreads / 32];
+    int32_t v[kScanTopItems];
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanTopItems; ++k) {
+        const int idx = threadIdx.x * kScanTopItems + k;
+        v[k] = idx < n ? count[idx] : 0;
+        local += v[k];
+    }
+    int32_t total;
+    int32_t run = block_exclusive_scan<kScanTopThreads>(local, warp_sums, &total);
+#pragma unroll
+    for (int k = 0; k < kScanTopItems; ++k) {
+        const int idx = threadIdx.x * kScanTopItems + k;
+        if (idx < n) start[idx] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) {
+        start[n] = total;
+        *n_next = total;
+    }
+    if (advance)
+        for (int s = threadIdx.x; s < nscenes; s += blockDim.x) scene_step[s] += 1;
+}
+
 void launch_scan(const LaunchCtx& L, int advance) {
     const int n = L.total_cells;
+    if (n <= kScanTopThreads * kScanTopItems) {
+        k_scan_single<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.count, n, L.sc.start, L.n_next, L.sc.scene_step,
+                                                           L.nscenes, advance);
+        return;
+    }
     const int ntiles = (n + kScanTile - 1) / kScanTile;
     k_scan_tiles<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
     k_scan_top<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
@@ -323,7 +361,8 @@ void launch_scan(const LaunchCtx& L, int advance) {
 void launch_place(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
     k_fill<<<grid, 128, 0, L.stream>>>(L.sc, L.st.id, L.cap);
-#define SPH_PLACE(D, T, SH) k_place<D, T, SH><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.st2, L.sc, L.cap)
+#define SPH_PLACE(D, T, SH) \
+    k_place<D, T, SH><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.st2, L.sc, L.cap, L.total_cells)
     const bool sh = L.precision == SPH_PRECISION_FP32_COMPENSATED;
     if (L.dim == 2) {
         if (L.thermal) { if (sh) SPH_PLACE(2, true, true); else SPH_PLACE(2, true, false); }

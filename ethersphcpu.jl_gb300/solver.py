@@ -168,6 +168,16 @@ class Simulation:
         self._check(self.lib.sph_download_ids(self.h, cap, C.byref(n), ids.ctypes.data_as(C.POINTER(C.c_int64))))
         return ids[: n.value]
 
+    def autotune(self, reps: int = 5) -> tuple:
+        """Pick the fastest FP32 launch shape on the current state (state unchanged)."""
+        out = (C.c_int32 * 4)()
+        self._check(self.lib.sph_autotune(self.h, reps, out))
+        return tuple(out)
+
+    def set_launch_shape(self, continuity: int, momentum: int, reinit: int, block: int) -> None:
+        shape = (C.c_int32 * 4)(continuity, momentum, reinit, block)
+        self._check(self.lib.sph_set_launch_shape(self.h, shape))
+
     def stats(self) -> _abi.SphStats:
         s = _abi.SphStats()
         self._check(self.lib.sph_stats(self.h, C.byref(s)))

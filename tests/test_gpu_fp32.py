@@ -49,6 +49,41 @@ def test_fp32_form_within_1e4_after_1000_steps(pkg, name):
     assert np.array_equal(a["mass"], b["mass"])
 
 
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_every_lane_count(pkg, lanes):
+    # each lanes-per-particle variant of the three FP32 gathers, against the FP64 form
+    s = scenes_mod().natural_convection_2d(n=48)
+    ref = run(pkg, s, 120, 0)
+    with pkg.Simulation(s.params(precision=1), s.n_fluid, s.n_wall) as sim:
+        for w in s.walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(s.fluid)
+        sim.set_launch_shape(lanes, lanes, lanes, 64 if lanes < 4 else 256)
+        sim.step(1, 120)
+        got = sim.download()
+    for k in ("rho", "v", "x", "t"):
+        assert rel(got[k], ref[k]) <= TOL_1000, (k, rel(got[k], ref[k]))
+
+
+def test_autotune_keeps_state(pkg):
+    s = scenes_mod().dam_break_2d(dx=0.02)
+    with pkg.Simulation(s.params(precision=1), s.n_fluid, s.n_wall) as sim:
+        for w in s.walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(s.fluid)
+        sim.step(1, 10)
+        before = sim.download()
+        shape = sim.autotune(2)
+        after = sim.download()
+        sim.step(11, 50)
+        cont = sim.download()
+    assert shape[0] in (1, 2, 4, 8) and shape[1] in (1, 2, 4, 8) and shape[3] in (64, 128, 256)
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    ref = run(pkg, s, 60, 0)
+    assert rel(cont["rho"], ref["rho"]) < 1e-6 and rel(cont["v"], ref["v"]) < 1e-4
+
+
 def test_fp32_form_repeatable(pkg):
     s = scenes_mod().natural_convection_2d(n=64)
     a = run(pkg, s, 200, 1)
