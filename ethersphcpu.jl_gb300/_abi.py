@@ -79,6 +79,15 @@ SIGNATURES = {
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
     "sph_count_pairs_noalloc": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
                                             C.c_void_p, C.c_void_p]),
+    "sph_batch_create": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                     C.POINTER(C.c_void_p)]),
+    "sph_batch_add_scene": (C.c_int32, [_H, C.POINTER(SphParams), C.c_int64, C.c_int64, C.c_int64] + [_DP] * 10 +
+                            [C.c_int64, C.POINTER(C.c_int32)] + [_DP] * 6 + [C.POINTER(C.c_int32)]),
+    "sph_batch_step": (C.c_int32, [_H, C.c_int64]),
+    "sph_batch_scene_info": (C.c_int32, [_H, C.c_int32, C.POINTER(C.c_int64)]),
+    "sph_batch_download_scene": (C.c_int32, [_H, C.c_int32, C.c_int64, C.POINTER(C.c_int64)] + [_DP] * 10),
+    "sph_batch_retire": (C.c_int32, [_H, C.c_int32]),
+    "sph_batch_free": (C.c_int32, [_H, C.POINTER(C.c_int64)]),
     "sph_autotune": (C.c_int32, [_H, C.c_int32, C.POINTER(C.c_int32)]),
     "sph_set_launch_shape": (C.c_int32, [_H, C.POINTER(C.c_int32)]),
     "sph_last_error": (C.c_char_p, [_H]),

@@ -190,12 +190,79 @@ bool scene_from_params(const SphParams& p, SceneDev& S, std::string& err) { retu
 void set_global_error(const std::string& msg) { g_create_error = msg; }
 }  // namespace sph
 
+namespace {
+
+// One simulation = one scene of the scene table.  Its cells are the range
+// [cell_off, cell_off + ncells] of the global cell space (the last cell is a sentinel
+// that never holds a particle, so start[] of the scene's cells never runs into another
+// scene's wall region), its walls the region [wall_off, wall_off + wall_n) of the wall
+// arrays, sorted by (cell, upload index).
+struct SceneRec {
+    bool used = false;
+    SceneDev dev{};
+    int32_t cell_span = 0;  // ncells + 1
+    int64_t wall_off = 0, wall_n = 0, wall_cap = 0;
+    int64_t first_step = 1;
+    int64_t step_host = 1;  // mirror of the scene's device step counter
+    std::vector<double> wx, wn, wv, wgap, wT, wkappa;  // host copy of the walls
+    std::vector<int32_t> wkind;
+};
+
+// First-fit allocator of ranges in [0, cap).
+struct RangeAlloc {
+    std::map<int64_t, int64_t> free_;  // offset -> length
+    void init(int64_t cap) {
+        free_.clear();
+        if (cap > 0) free_[0] = cap;
+    }
+    bool alloc(int64_t len, int64_t* off) {
+        if (len == 0) {
+            *off = 0;
+            return true;
+        }
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= len) {
+                *off = it->first;
+                const int64_t rest = it->second - len, at = it->first + len;
+                free_.erase(it);
+                if (rest > 0) free_[at] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(int64_t off, int64_t len) {
+        if (len == 0) return;
+        auto it = free_.emplace(off, len).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    int64_t largest() const {
+        int64_t m = 0;
+        for (auto& kv : free_) m = std::max(m, kv.second);
+        return m;
+    }
+};
+
+}  // namespace
+
 struct SphHandle {
-    SphParams prm{};
-    SceneDev scene{};
+    SphParams prm{};  // prototype (single-scene handles: the scene's parameters)
+    bool batch = false;
     int dim = 2, kernel = 0, mode = 0, thermal = 0, precision = 0;
     int64_t cap = 0, wcap = 0;
-    int32_t total_cells = 0;
+    int32_t total_cells = 0;  // cell capacity (the scan covers all of it)
+    int32_t scap = 1;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     SortedState S[2]{};
@@ -207,17 +274,16 @@ struct SphHandle {
     double* d_stat_partials = nullptr;
     double* d_stat_out = nullptr;
     unsigned long long* d_pair_counts = nullptr;
-    int64_t* h_pinned_step = nullptr;
+    int64_t* h_pinned = nullptr;  // [0]: step upload, [1]: status, [2..3]: ranges
     int par = 0;
-    int64_t dev_step = INT64_MIN;  // value of the device step counter (host mirror)
-    // FP32 launch shape: lanes per particle for continuity, momentum, Shepard; block size
-    int tune[4] = {4, 4, 4, 128};
     bool have_fluid = false;
     int64_t steps_done = 0;
+    // FP32 launch shape: lanes per particle for continuity, momentum, Shepard; block size
+    int tune[4] = {4, 4, 4, 128};
     std::string err;
-    std::vector<double> hwx, hwn, hwv, hwgap, hwT, hwkappa;
-    std::vector<int32_t> hwkind;
-    // graph cache: key = (parity, pattern of reinit flags) -> executable graph
+    std::vector<SceneRec> scenes;
+    RangeAlloc cells, walls;
+    // graph cache: key = (parity, pattern of Shepard steps) -> executable graph
     std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
 };
 
@@ -252,16 +318,19 @@ cudaError_t dalloc(SphHandle* h, T** p, size_t count) {
 
 size_t vec_bytes(int dim) { return dim == 2 ? sizeof(double2) : sizeof(double4); }
 
+cudaError_t alloc_vec(SphHandle* h, void** p, size_t n) {
+    const size_t bytes = std::max<size_t>(n, 1) * vec_bytes(h->dim);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return e;
+    h->allocs.push_back(*p);
+    return cudaMemsetAsync(*p, 0, bytes, h->stream);
+}
+
 cudaError_t alloc_sorted(SphHandle* h, SortedState& s) {
     const size_t n = (size_t)h->cap;
     cudaError_t e;
-    void* q;
-    if ((e = cudaMalloc(&q, n * vec_bytes(h->dim) + 16)) != cudaSuccess) return e;
-    h->allocs.push_back(q);
-    s.x = q;
-    if ((e = cudaMalloc(&q, n * vec_bytes(h->dim) + 16)) != cudaSuccess) return e;
-    h->allocs.push_back(q);
-    s.v = q;
+    if ((e = alloc_vec(h, &s.x, n)) != cudaSuccess) return e;
+    if ((e = alloc_vec(h, &s.v, n)) != cudaSuccess) return e;
     double** d[] = {&s.rho, &s.rhoc, &s.p, &s.c, &s.P, &s.m, &s.gap};
     for (double** pp : d)
         if ((e = dalloc(h, pp, n)) != cudaSuccess) return e;
@@ -293,7 +362,7 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.precision = h->precision;
     L.cap = (int32_t)h->cap;
     L.total_cells = h->total_cells;
-    L.nscenes = 1;
+    L.nscenes = h->scap;
     L.scenes = h->d_scenes;
     L.st = h->S[h->par];
     L.st2 = h->S[h->par ^ 1];
@@ -315,11 +384,11 @@ void launch_physics(int stage, const LaunchCtx& L) {
     else launch_physics_fp32(stage, L);
 }
 
-// Enqueue one step (no synchronisation).  `reinit` must equal the device-side
-// decision for the step (the kernel re-checks it per scene).
+// Enqueue one step (no synchronisation).  `reinit`: some running scene re-initialises
+// its density at this step (the kernel decides per scene).
 void enqueue_step(SphHandle* h, bool reinit) {
     LaunchCtx L = make_ctx(h);
-    // count[] was zeroed by the previous placement (or by the upload)
+    // count[] was zeroed by the previous placement (or by the last re-sort)
     launch_physics(0, L);
     launch_physics(1, L);
     if (reinit) launch_physics(2, L);
@@ -328,8 +397,14 @@ void enqueue_step(SphHandle* h, bool reinit) {
     h->par ^= 1;
 }
 
-int sort_after_upload(SphHandle* h) {
+// Sort the current state S[par] (n_live particles, possibly unsorted after an upload
+// or with retired scenes to drop) into S[par^1] and swap.
+int resort(SphHandle* h) {
     LaunchCtx L = make_ctx(h);
+    L.nx.x = L.st.x;
+    L.nx.v = L.st.v;
+    L.nx.rho = L.st.rho;
+    L.nx.T = L.st.T;
     SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, h->stream));
     launch_hash(L);
     launch_scan(L, 0);
@@ -342,91 +417,157 @@ int sort_after_upload(SphHandle* h) {
 
 bool is_step_host(int64_t step, int64_t interval) { return interval > 0 && step % interval == 0; }
 
-}  // namespace
-
-extern "C" {
-
-int32_t sph_version(void) { return SPH_ABI_VERSION; }
-
-int32_t sph_create(const SphParams* params, int64_t fluid_capacity, int64_t wall_capacity, SphHandle** out) {
-    if (!params || !out) return fail(nullptr, SPH_ERR_ARG, "null argument");
-    *out = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(nullptr, SPH_ERR_NO_DEVICE, "no CUDA device");
-    if (fluid_capacity < 1 || fluid_capacity > (int64_t)INT32_MAX / 2 || wall_capacity < 0 ||
-        wall_capacity > (int64_t)INT32_MAX / 2)
-        return fail(nullptr, SPH_ERR_ARG, "capacity out of range");
-    SceneDev S;
-    std::string err;
-    if (!build_scene(*params, S, err)) return fail(nullptr, SPH_ERR_ARG, err);
-
-    SphHandle* h = new SphHandle();
-    h->prm = *params;
-    h->scene = S;
-    h->dim = params->dim;
-    h->kernel = params->kernel;
-    h->mode = mode_of(params->solve);
-    h->thermal = params->thermal;
-    h->precision = params->precision;
-    h->cap = fluid_capacity;
-    h->wcap = wall_capacity;
-    h->total_cells = S.ncells;
-    int rc = SPH_OK;
-    auto bail = [&](cudaError_t e, const char* what) {
-        rc = cuda_fail(nullptr, e, what);
-        sph_destroy(h);
-        return rc;
-    };
-    cudaError_t e;
-    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
-    for (int b = 0; b < 2; ++b)
-        if ((e = alloc_sorted(h, h->S[b])) != cudaSuccess) return bail(e, "sorted state");
-    {
-        void* q;
-        if ((e = cudaMalloc(&q, (size_t)h->cap * vec_bytes(h->dim) + 16)) != cudaSuccess) return bail(e, "next x");
-        h->allocs.push_back(q);
-        h->N.x = q;
-        if ((e = cudaMalloc(&q, (size_t)h->cap * vec_bytes(h->dim) + 16)) != cudaSuccess) return bail(e, "next v");
-        h->allocs.push_back(q);
-        h->N.v = q;
-        if ((e = dalloc(h, &h->N.rho, h->cap)) != cudaSuccess) return bail(e, "next rho");
-        if (h->thermal && (e = dalloc(h, &h->N.T, h->cap)) != cudaSuccess) return bail(e, "next T");
-    }
-    const size_t ncell = (size_t)h->total_cells;
-    if ((e = dalloc(h, &h->sc.key, h->cap)) != cudaSuccess) return bail(e, "key");
-    if ((e = dalloc(h, &h->sc.slot, h->cap)) != cudaSuccess) return bail(e, "slot");
-    if ((e = dalloc(h, &h->sc.tmp, h->cap)) != cudaSuccess) return bail(e, "tmp");
-    if ((e = dalloc(h, &h->sc.count, ncell)) != cudaSuccess) return bail(e, "count");
-    if ((e = dalloc(h, &h->sc.start, ncell + 1)) != cudaSuccess) return bail(e, "start");
-    if ((e = dalloc(h, &h->sc.block_sums, ncell / 4096 + 2)) != cudaSuccess) return bail(e, "block sums");
-    if ((e = dalloc(h, &h->sc.status, 1)) != cudaSuccess) return bail(e, "status");
-    if ((e = dalloc(h, &h->sc.scene_step, 1)) != cudaSuccess) return bail(e, "scene step");
-    if ((e = dalloc(h, &h->nbuf, 2)) != cudaSuccess) return bail(e, "counters");
-    if ((e = dalloc(h, &h->W.start, ncell + 1)) != cudaSuccess) return bail(e, "wall start");
-    if ((e = dalloc(h, &h->d_scenes, 1)) != cudaSuccess) return bail(e, "scenes");
-    if ((e = dalloc(h, &h->d_stat_partials, 3 * 152)) != cudaSuccess) return bail(e, "stats");
-    if ((e = dalloc(h, &h->d_stat_out, 4)) != cudaSuccess) return bail(e, "stats");
-    if ((e = dalloc(h, &h->d_pair_counts, 2)) != cudaSuccess) return bail(e, "pairs");
-    if ((e = cudaMallocHost((void**)&h->h_pinned_step, sizeof(int64_t) * 2)) != cudaSuccess) return bail(e, "pinned");
-    if ((e = cudaMemcpyAsync(h->d_scenes, &h->scene, sizeof(SceneDev), cudaMemcpyHostToDevice, h->stream)) !=
-        cudaSuccess)
-        return bail(e, "scene upload");
-    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(e, "create sync");
-    *out = h;
+int32_t read_live(SphHandle* h, int32_t* n) {
+    SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned[2], h->nbuf + h->par, 4, cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::memcpy(n, &h->h_pinned[2], 4);
     return SPH_OK;
 }
 
-int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double* v, const double* rho,
-                         const double* p, const double* c, const double* mass, const double* gap, const double* t,
-                         const double* kappa, const double* cp) {
-    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
-    if (n < 0 || n > h->cap) return fail(h, SPH_ERR_GRID_OVERFLOW, "fluid count exceeds the handle capacity");
+// [begin, end) of scene s in the sorted arrays.
+int32_t scene_range(SphHandle* h, int s, int32_t* b, int32_t* e) {
+    const SceneRec& R = h->scenes[s];
+    int32_t v[2];
+    SPH_CUDA(h, cudaMemcpyAsync(&v[0], h->sc.start + R.dev.cell_off, 4, cudaMemcpyDeviceToHost, h->stream));
+    SPH_CUDA(h, cudaMemcpyAsync(&v[1], h->sc.start + R.dev.cell_off + R.dev.ncells, 4, cudaMemcpyDeviceToHost,
+                                h->stream));
+    SPH_CUDA(h, cudaStreamSynchronize(h->stream));
+    *b = v[0];
+    *e = v[1];
+    return SPH_OK;
+}
+
+int32_t upload_scene_const(SphHandle* h, int s) {
+    SPH_CUDA(h, cudaMemcpyAsync(h->d_scenes + s, &h->scenes[s].dev, sizeof(SceneDev), cudaMemcpyHostToDevice,
+                                h->stream));
+    return SPH_OK;
+}
+
+int32_t set_scene_step(SphHandle* h, int s, int64_t step) {
+    h->h_pinned[0] = step;
+    SPH_CUDA(h, cudaMemcpyAsync(h->sc.scene_step + s, &h->h_pinned[0], 8, cudaMemcpyHostToDevice, h->stream));
+    SPH_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->scenes[s].step_host = step;
+    return SPH_OK;
+}
+
+// Write the walls of scene s (host copy) into its region: sorted by (cell, upload
+// index), with the scene's wall cell starts and FP32 shadows.
+int32_t write_scene_walls(SphHandle* h, int s) {
+    SceneRec& R = h->scenes[s];
+    const SceneDev& S = R.dev;
+    const int dim = h->dim;
+    const int64_t nw = (int64_t)R.wgap.size();
+    std::vector<int32_t> key(nw);
+    for (int64_t w = 0; w < nw; ++w) key[w] = host_cell_key(S, dim, &R.wx[w * dim]);
+    std::vector<int64_t> order(nw);
+    for (int64_t w = 0; w < nw; ++w) order[w] = w;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+    std::vector<int32_t> start(R.cell_span, 0);  // ncells + 1 entries
+    for (int64_t w = 0; w < nw; ++w) start[key[w] - S.cell_off + 1]++;
+    for (int32_t c = 0; c + 1 < R.cell_span; ++c) start[c + 1] += start[c];
+    for (auto& v : start) v += (int32_t)R.wall_off;
+    const size_t vb = vec_bytes(dim);
+    std::vector<char> bx(nw * vb, 0), bn(nw * vb, 0), bv(nw * vb, 0);
+    std::vector<double> bg(nw), bT(nw), bk(nw);
+    std::vector<int32_t> bkind(nw);
+    std::vector<float4> fa, fb, fc;
+    const bool shadow = h->precision == SPH_PRECISION_FP32_COMPENSATED;
+    if (shadow) {
+        fa.resize(nw);
+        fb.resize(nw);
+        fc.resize(nw);
+    }
+    for (int64_t q = 0; q < nw; ++q) {
+        const int64_t w = order[q];
+        for (int k = 0; k < dim; ++k) {
+            ((double*)(bx.data() + q * vb))[k] = R.wx[w * dim + k];
+            ((double*)(bn.data() + q * vb))[k] = R.wn[w * dim + k];
+            ((double*)(bv.data() + q * vb))[k] = R.wv[w * dim + k];
+        }
+        bg[q] = R.wgap[w];
+        bT[q] = R.wT[w];
+        bk[q] = R.wkappa[w];
+        bkind[q] = R.wkind[w];
+        if (shadow) {  // position relative to the origin of the wall's cell
+            const int32_t k = key[w] - S.cell_off;
+            const int32_t cc[3] = {k % S.n[0], (k / S.n[0]) % S.n[1], k / (S.n[0] * S.n[1])};
+            float xr[3] = {0.f, 0.f, 0.f}, nr[3] = {0.f, 0.f, 0.f}, vr[3] = {0.f, 0.f, 0.f};
+            for (int a = 0; a < dim; ++a) {
+                xr[a] = (float)(R.wx[w * dim + a] - (S.lo[a] + (double)cc[a] * S.cell_d[a]));
+                nr[a] = (float)R.wn[w * dim + a];
+                vr[a] = (float)R.wv[w * dim + a];
+            }
+            const float g = (float)R.wgap[w], T = (float)R.wT[w], kap = (float)R.wkappa[w];
+            const float thermo = R.wkind[w] == SPH_WALL_THERMOSTATIC ? 1.f : 0.f;
+            if (dim == 2) {
+                fa[q] = make_float4(xr[0], xr[1], nr[0], nr[1]);
+                fb[q] = make_float4(vr[0], vr[1], g, T);
+                fc[q] = make_float4(kap, thermo, 0.f, 0.f);
+            } else {
+                fa[q] = make_float4(xr[0], xr[1], xr[2], g);
+                fb[q] = make_float4(nr[0], nr[1], nr[2], T);
+                fc[q] = make_float4(vr[0], vr[1], vr[2], kap);
+            }
+        }
+    }
+    cudaStream_t st = h->stream;
+    const int64_t o = R.wall_off;
+    if (nw > 0) {
+        SPH_CUDA(h, cudaMemcpyAsync((char*)h->W.x + o * vb, bx.data(), nw * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync((char*)h->W.nrm + o * vb, bn.data(), nw * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync((char*)h->W.v + o * vb, bv.data(), nw * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->W.gap + o, bg.data(), nw * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->W.T + o, bT.data(), nw * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->W.kappa + o, bk.data(), nw * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->W.kind + o, bkind.data(), nw * 4, cudaMemcpyHostToDevice, st));
+        if (shadow) {
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fa + o, fa.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fb + o, fb.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(h->W.fc + o, fc.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
+        }
+    }
+    SPH_CUDA(h, cudaMemcpyAsync(h->W.start + S.cell_off, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    R.wall_n = nw;
+    return SPH_OK;
+}
+
+// Append walls to the host copy of scene s.
+int32_t add_walls_host(SphHandle* h, SceneRec& R, int32_t kind, int64_t n, const double* x, const double* normal,
+                       const double* gap, const double* t, const double* kappa, const double* v) {
+    const int dim = h->dim;
+    if (kind < SPH_WALL_COMPULSIVE || kind > SPH_WALL_THERMOSTATIC) return fail(h, SPH_ERR_ARG, "unknown wall kind");
+    if (n < 0) return fail(h, SPH_ERR_ARG, "negative wall count");
+    if (n > 0 && (!x || !normal || !gap)) return fail(h, SPH_ERR_ARG, "wall x, normal, gap are required");
+    if (n > 0 && kind == SPH_WALL_THERMOSTATIC && (!t || !kappa))
+        return fail(h, SPH_ERR_ARG, "thermostatic walls need t and kappa");
+    if (n > 0 && kind == SPH_WALL_STATIC_VELOCITY && !v) return fail(h, SPH_ERR_ARG, "velocity walls need v");
+    for (int64_t i = 0; i < n; ++i) {
+        for (int k = 0; k < dim; ++k) {
+            R.wx.push_back(x[i * dim + k]);
+            R.wn.push_back(normal[i * dim + k]);
+            R.wv.push_back(kind == SPH_WALL_STATIC_VELOCITY ? v[i * dim + k] : 0.0);
+        }
+        R.wgap.push_back(gap[i]);
+        R.wT.push_back(kind == SPH_WALL_THERMOSTATIC ? t[i] : 0.0);
+        R.wkappa.push_back(kind == SPH_WALL_THERMOSTATIC ? kappa[i] : 0.0);
+        R.wkind.push_back(kind);
+    }
+    return SPH_OK;
+}
+
+// Append n fluid particles of scene s at the end of the live range of S[par] (ids
+// 0..n-1 within the scene), then re-sort.
+int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const double* x, const double* v,
+                     const double* rho, const double* p, const double* c, const double* mass, const double* gap,
+                     const double* t, const double* kappa, const double* cp) {
+    const int dim = h->dim;
+    const SceneDev& S = h->scenes[s].dev;
+    if ((int64_t)n_before + n > h->cap) return fail(h, SPH_ERR_OOM, "fluid count exceeds the handle capacity");
     if (n > 0 && (!x || !v || !rho || !mass || !gap)) return fail(h, SPH_ERR_ARG, "x, v, rho, mass, gap are required");
     if (n > 0 && h->thermal && (!t || !kappa || !cp))
         return fail(h, SPH_ERR_ARG, "thermal particles need t, kappa and cp");
-    const int dim = h->dim;
-    const SceneDev& S = h->scene;
-    // staging in the device layout
     const size_t vb = vec_bytes(dim);
     std::vector<char> hx(n * vb), hv(n * vb);
     for (int64_t i = 0; i < n; ++i) {
@@ -449,184 +590,102 @@ int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double*
             hc[i] = S.c0 * std::sqrt(host_powi(rr, S.gamma - 1));
         }
     }
-    std::vector<int32_t> ids(n), scn(n, 0);
+    std::vector<int32_t> ids(n), scn(n, s);
     for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
-    bool uniform = true;
-    for (int64_t i = 1; i < n; ++i) uniform &= gap[i] == gap[0];
-    h->scene.uniform_gap = uniform ? 1 : 0;
-
-    SortedState& s = h->S[h->par];
+    SortedState& d = h->S[h->par];
     cudaStream_t st = h->stream;
-    const int32_t n32 = (int32_t)n;
-    SPH_CUDA(h, cudaMemcpyAsync(h->d_scenes, &h->scene, sizeof(SceneDev), cudaMemcpyHostToDevice, st));
+    const size_t o = (size_t)n_before;
     if (n > 0) {
-        SPH_CUDA(h, cudaMemcpyAsync(h->N.x, hx.data(), n * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->N.v, hv.data(), n * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->N.rho, rho, n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.p, hp.data(), n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.c, hc.data(), n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.m, mass, n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.gap, gap, n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.id, ids.data(), n * 4, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(s.scene, scn.data(), n * 4, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync((char*)d.x + o * vb, hx.data(), n * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync((char*)d.v + o * vb, hv.data(), n * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.rho + o, rho, n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.p + o, hp.data(), n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.c + o, hc.data(), n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.m + o, mass, n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.gap + o, gap, n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.id + o, ids.data(), n * 4, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.scene + o, scn.data(), n * 4, cudaMemcpyHostToDevice, st));
         if (h->thermal) {
-            SPH_CUDA(h, cudaMemcpyAsync(h->N.T, t, n * 8, cudaMemcpyHostToDevice, st));
-            SPH_CUDA(h, cudaMemcpyAsync(s.kappa, kappa, n * 8, cudaMemcpyHostToDevice, st));
-            SPH_CUDA(h, cudaMemcpyAsync(s.cp, cp, n * 8, cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(d.T + o, t, n * 8, cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(d.kappa + o, kappa, n * 8, cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(d.cp + o, cp, n * 8, cudaMemcpyHostToDevice, st));
         }
     }
-    SPH_CUDA(h, cudaMemcpyAsync(h->nbuf + h->par, &n32, 4, cudaMemcpyHostToDevice, st));
+    h->h_pinned[2] = 0;
+    const int32_t total = (int32_t)(n_before + n);
+    std::memcpy(&h->h_pinned[2], &total, 4);
+    SPH_CUDA(h, cudaMemcpyAsync(h->nbuf + h->par, &h->h_pinned[2], 4, cudaMemcpyHostToDevice, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));  // host staging buffers die at return
-    int rc = sort_after_upload(h);
-    if (rc != SPH_OK) return rc;
-    h->have_fluid = true;
-    return SPH_OK;
+    return resort(h);
 }
 
-int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x, const double* normal,
-                         const double* gap, const double* t, const double* kappa, const double* v) {
-    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
-    if (kind < SPH_WALL_COMPULSIVE || kind > SPH_WALL_THERMOSTATIC) return fail(h, SPH_ERR_ARG, "unknown wall kind");
-    if (n < 0) return fail(h, SPH_ERR_ARG, "negative wall count");
-    if (n > 0 && (!x || !normal || !gap)) return fail(h, SPH_ERR_ARG, "x, normal, gap are required");
-    if (n > 0 && kind == SPH_WALL_THERMOSTATIC && (!t || !kappa))
-        return fail(h, SPH_ERR_ARG, "thermostatic walls need t and kappa");
-    if (n > 0 && kind == SPH_WALL_STATIC_VELOCITY && !v) return fail(h, SPH_ERR_ARG, "velocity walls need v");
-    const int dim = h->dim;
-    const int64_t total = (int64_t)h->hwgap.size() + n;
-    if (total > h->wcap) return fail(h, SPH_ERR_GRID_OVERFLOW, "wall count exceeds the handle capacity");
-    for (int64_t i = 0; i < n; ++i) {
-        for (int k = 0; k < dim; ++k) {
-            h->hwx.push_back(x[i * dim + k]);
-            h->hwn.push_back(normal[i * dim + k]);
-            h->hwv.push_back(kind == SPH_WALL_STATIC_VELOCITY ? v[i * dim + k] : 0.0);
-        }
-        h->hwgap.push_back(gap[i]);
-        h->hwT.push_back(kind == SPH_WALL_THERMOSTATIC ? t[i] : 0.0);
-        h->hwkappa.push_back(kind == SPH_WALL_THERMOSTATIC ? kappa[i] : 0.0);
-        h->hwkind.push_back(kind);
-    }
-    // sort all walls by (cell, upload index) and build the wall cell list on the host
-    const int64_t nw = total;
-    std::vector<int32_t> key(nw);
-    for (int64_t w = 0; w < nw; ++w) key[w] = host_cell_key(h->scene, dim, &h->hwx[w * dim]);
-    std::vector<int64_t> order(nw);
-    for (int64_t w = 0; w < nw; ++w) order[w] = w;
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
-    std::vector<int32_t> start(h->total_cells + 1, 0);
-    for (int64_t w = 0; w < nw; ++w) start[key[w] + 1]++;
-    for (int32_t c = 0; c < h->total_cells; ++c) start[c + 1] += start[c];
-    const size_t vb = vec_bytes(dim);
-    std::vector<char> bx(nw * vb, 0), bn(nw * vb, 0), bv(nw * vb, 0);
-    std::vector<double> bg(nw), bT(nw), bk(nw);
-    std::vector<int32_t> bkind(nw);
-    for (int64_t q = 0; q < nw; ++q) {
-        const int64_t w = order[q];
-        for (int k = 0; k < dim; ++k) {
-            ((double*)(bx.data() + q * vb))[k] = h->hwx[w * dim + k];
-            ((double*)(bn.data() + q * vb))[k] = h->hwn[w * dim + k];
-            ((double*)(bv.data() + q * vb))[k] = h->hwv[w * dim + k];
-        }
-        bg[q] = h->hwgap[w];
-        bT[q] = h->hwT[w];
-        bk[q] = h->hwkappa[w];
-        bkind[q] = h->hwkind[w];
-    }
-    // (re)allocate wall arrays to the full capacity once
-    if (!h->W.x) {
-        const size_t cap = (size_t)std::max<int64_t>(h->wcap, 1);
-        void* q;
-        SPH_CUDA(h, cudaMalloc(&q, cap * vb));
-        h->allocs.push_back(q);
-        h->W.x = q;
-        SPH_CUDA(h, cudaMalloc(&q, cap * vb));
-        h->allocs.push_back(q);
-        h->W.nrm = q;
-        SPH_CUDA(h, cudaMalloc(&q, cap * vb));
-        h->allocs.push_back(q);
-        h->W.v = q;
-        SPH_CUDA(h, dalloc(h, &h->W.gap, cap));
-        SPH_CUDA(h, dalloc(h, &h->W.T, cap));
-        SPH_CUDA(h, dalloc(h, &h->W.kappa, cap));
-        SPH_CUDA(h, dalloc(h, &h->W.kind, cap));
-    }
+// Download the live particles of scene s in ascending id.
+int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, double* x, double* v, double* rho,
+                       double* p, double* c, double* mass, double* gap, double* t, double* kappa, double* cp,
+                       int64_t* ids_out) {
+    int32_t b = 0, e = 0;
+    int32_t rc = scene_range(h, s, &b, &e);
+    if (rc != SPH_OK) return rc;
+    const int64_t n = e - b;
+    *n_out = n;
+    if (n > capacity) return fail(h, SPH_ERR_ARG, "caller arrays too small for the live fluid");
+    if (n == 0) return SPH_OK;
     cudaStream_t st = h->stream;
-    if (nw > 0) {
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.x, bx.data(), nw * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.nrm, bn.data(), nw * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.v, bv.data(), nw * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.gap, bg.data(), nw * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.T, bT.data(), nw * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.kappa, bk.data(), nw * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(h->W.kind, bkind.data(), nw * 4, cudaMemcpyHostToDevice, st));
+    const int dim = h->dim;
+    const SortedState& d = h->S[h->par];
+    const size_t vb = vec_bytes(dim);
+    std::vector<int32_t> ids(n);
+    SPH_CUDA(h, cudaMemcpyAsync(ids.data(), d.id + b, n * 4, cudaMemcpyDeviceToHost, st));
+    std::vector<char> bx, bv;
+    std::vector<double> b1[8];
+    const double* srcs[8] = {d.rho, d.p, d.c, d.m, d.gap, d.T, d.kappa, d.cp};
+    double* dsts[8] = {rho, p, c, mass, gap, t, kappa, cp};
+    if (x) {
+        bx.resize(n * vb);
+        SPH_CUDA(h, cudaMemcpyAsync(bx.data(), (const char*)d.x + (size_t)b * vb, n * vb, cudaMemcpyDeviceToHost, st));
     }
-    SPH_CUDA(h, cudaMemcpyAsync(h->W.start, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st));
-    std::vector<float4> fa, fb, fc;
-    if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
-        // FP32 wall shadows, positions relative to the origin of the wall's cell
-        const SceneDev& S = h->scene;
-        if (!h->W.fa) {
-            const size_t cap = (size_t)std::max<int64_t>(h->wcap, 1);
-            SPH_CUDA(h, dalloc(h, &h->W.fa, cap));
-            SPH_CUDA(h, dalloc(h, &h->W.fb, cap));
-            SPH_CUDA(h, dalloc(h, &h->W.fc, cap));
-        }
-        fa.resize(nw);
-        fb.resize(nw);
-        fc.resize(nw);
-        for (int64_t q = 0; q < nw; ++q) {
-            const int64_t w = order[q];
-            const int32_t k = key[w] - S.cell_off;
-            const int32_t cc[3] = {k % S.n[0], (k / S.n[0]) % S.n[1], k / (S.n[0] * S.n[1])};
-            float xr[3] = {0.f, 0.f, 0.f}, nr[3] = {0.f, 0.f, 0.f}, vr[3] = {0.f, 0.f, 0.f};
-            for (int a = 0; a < dim; ++a) {
-                xr[a] = (float)(h->hwx[w * dim + a] - (S.lo[a] + (double)cc[a] * S.cell_d[a]));
-                nr[a] = (float)h->hwn[w * dim + a];
-                vr[a] = (float)h->hwv[w * dim + a];
-            }
-            const float g = (float)h->hwgap[w], T = (float)h->hwT[w], kap = (float)h->hwkappa[w];
-            const float thermo = h->hwkind[w] == SPH_WALL_THERMOSTATIC ? 1.f : 0.f;
-            if (dim == 2) {
-                fa[q] = make_float4(xr[0], xr[1], nr[0], nr[1]);
-                fb[q] = make_float4(vr[0], vr[1], g, T);
-                fc[q] = make_float4(kap, thermo, 0.f, 0.f);
-            } else {
-                fa[q] = make_float4(xr[0], xr[1], xr[2], g);
-                fb[q] = make_float4(nr[0], nr[1], nr[2], T);
-                fc[q] = make_float4(vr[0], vr[1], vr[2], kap);
-            }
-        }
-        if (nw > 0) {
-            SPH_CUDA(h, cudaMemcpyAsync(h->W.fa, fa.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
-            SPH_CUDA(h, cudaMemcpyAsync(h->W.fb, fb.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
-            SPH_CUDA(h, cudaMemcpyAsync(h->W.fc, fc.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, st));
-        }
+    if (v) {
+        bv.resize(n * vb);
+        SPH_CUDA(h, cudaMemcpyAsync(bv.data(), (const char*)d.v + (size_t)b * vb, n * vb, cudaMemcpyDeviceToHost, st));
+    }
+    for (int f = 0; f < 8; ++f) {
+        if (!dsts[f] || !srcs[f]) continue;
+        b1[f].resize(n);
+        SPH_CUDA(h, cudaMemcpyAsync(b1[f].data(), srcs[f] + b, n * 8, cudaMemcpyDeviceToHost, st));
     }
     SPH_CUDA(h, cudaStreamSynchronize(st));
-    h->W.n = nw;
-    // the captured graphs hold the old wall state
-    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-    h->graphs.clear();
+    // ascending id = the caller's original order with deleted particles removed
+    std::vector<int64_t> order(n);
+    for (int64_t k = 0; k < n; ++k) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t q) { return ids[a] < ids[q]; });
+    for (int64_t q = 0; q < n; ++q) {
+        const int64_t k = order[q];
+        for (int a = 0; a < dim; ++a) {
+            if (x) x[q * dim + a] = ((const double*)(bx.data() + k * vb))[a];
+            if (v) v[q * dim + a] = ((const double*)(bv.data() + k * vb))[a];
+        }
+        for (int f = 0; f < 8; ++f)
+            if (dsts[f] && srcs[f]) dsts[f][q] = b1[f][k];
+        if (ids_out) ids_out[q] = ids[k];
+    }
     return SPH_OK;
 }
 
-int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
-    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
-    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_step before sph_upload_fluid");
-    if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
-    if (nsteps == 0) return SPH_OK;
+// Run nsteps steps of every scene (each at its own step number) as CUDA-graph bundles.
+int32_t step_all_async(SphHandle* h, int64_t nsteps) {
     cudaStream_t st = h->stream;
-    if (first_step != h->dev_step) {  // the device step counter only needs a reset on a jump
-        h->h_pinned_step[0] = first_step;
-        SPH_CUDA(h, cudaMemcpyAsync(h->sc.scene_step, h->h_pinned_step, 8, cudaMemcpyHostToDevice, st));
-    }
     const int64_t bundle = 10;
-    int64_t s = first_step;
-    const int64_t end = first_step + nsteps;
-    while (s < end) {
-        const int64_t nb = std::min(bundle, end - s);
-        std::vector<bool> pattern(nb);
-        for (int64_t q = 0; q < nb; ++q) pattern[q] = is_step_host(s + q, h->scene.reinit_interval);
+    int64_t done = 0;
+    while (done < nsteps) {
+        const int64_t nb = std::min(bundle, nsteps - done);
+        std::vector<bool> pattern(nb, false);
+        for (const SceneRec& R : h->scenes) {
+            if (!R.used || !R.dev.active) continue;
+            for (int64_t q = 0; q < nb; ++q) {
+                const int64_t s = R.step_host + done + q;
+                if (s <= R.dev.last_step && is_step_host(s, R.dev.reinit_interval)) pattern[q] = true;
+            }
+        }
         auto key = std::make_pair(h->par, pattern);
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
@@ -649,22 +708,199 @@ int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
         }
         SPH_CUDA(h, cudaGraphLaunch(it->second, st));
         if (nb & 1) h->par ^= 1;
-        s += nb;
+        done += nb;
     }
-    h->dev_step = end;
+    for (SceneRec& R : h->scenes)
+        if (R.used) R.step_host += nsteps;
     h->steps_done += nsteps;
     return SPH_OK;
+}
+
+int32_t allocate_handle(SphHandle* h, int64_t cells) {
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "stream");
+    for (int b = 0; b < 2; ++b)
+        if ((e = alloc_sorted(h, h->S[b])) != cudaSuccess) return cuda_fail(nullptr, e, "sorted state");
+    if ((e = alloc_vec(h, &h->N.x, h->cap)) != cudaSuccess) return cuda_fail(nullptr, e, "next x");
+    if ((e = alloc_vec(h, &h->N.v, h->cap)) != cudaSuccess) return cuda_fail(nullptr, e, "next v");
+    if ((e = dalloc(h, &h->N.rho, h->cap)) != cudaSuccess) return cuda_fail(nullptr, e, "next rho");
+    if (h->thermal && (e = dalloc(h, &h->N.T, h->cap)) != cudaSuccess) return cuda_fail(nullptr, e, "next T");
+    const size_t ncell = (size_t)cells;
+    const size_t wc = (size_t)std::max<int64_t>(h->wcap, 1);
+    struct {
+        int32_t** p;
+        size_t n;
+    } ints[] = {{&h->sc.key, (size_t)h->cap},        {&h->sc.slot, (size_t)h->cap},
+                {&h->sc.tmp, (size_t)h->cap},        {&h->sc.count, ncell},
+                {&h->sc.start, ncell + 1},           {&h->sc.block_sums, ncell / 4096 + 2},
+                {&h->sc.status, 1},                  {&h->nbuf, 2},
+                {&h->W.start, ncell + 1},            {&h->W.kind, wc}};
+    for (auto& a : ints)
+        if ((e = dalloc(h, a.p, a.n)) != cudaSuccess) return cuda_fail(nullptr, e, "scratch");
+    if ((e = dalloc(h, &h->sc.scene_step, (size_t)h->scap)) != cudaSuccess) return cuda_fail(nullptr, e, "steps");
+    if ((e = dalloc(h, &h->d_scenes, (size_t)h->scap)) != cudaSuccess) return cuda_fail(nullptr, e, "scenes");
+    if ((e = alloc_vec(h, &h->W.x, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if ((e = alloc_vec(h, &h->W.nrm, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if ((e = alloc_vec(h, &h->W.v, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if ((e = dalloc(h, &h->W.gap, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if ((e = dalloc(h, &h->W.T, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if ((e = dalloc(h, &h->W.kappa, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
+        if ((e = dalloc(h, &h->W.fa, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+        if ((e = dalloc(h, &h->W.fb, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+        if ((e = dalloc(h, &h->W.fc, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");
+    }
+    if ((e = dalloc(h, &h->d_stat_partials, 3 * 152)) != cudaSuccess) return cuda_fail(nullptr, e, "stats");
+    if ((e = dalloc(h, &h->d_stat_out, 4)) != cudaSuccess) return cuda_fail(nullptr, e, "stats");
+    if ((e = dalloc(h, &h->d_pair_counts, 2)) != cudaSuccess) return cuda_fail(nullptr, e, "pairs");
+    if ((e = cudaMallocHost((void**)&h->h_pinned, sizeof(int64_t) * 4)) != cudaSuccess)
+        return cuda_fail(nullptr, e, "pinned");
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return cuda_fail(nullptr, e, "create sync");
+    h->total_cells = (int32_t)cells;
+    h->cells.init(cells);
+    h->walls.init(h->wcap);
+    h->scenes.assign(h->scap, SceneRec());
+    h->W.n = 1;  // wall walks read the (possibly empty) ranges of every scene
+    return SPH_OK;
+}
+
+bool same_kind(const SphHandle* h, const SphParams& p) {
+    return p.dim == h->dim && p.kernel == h->kernel && mode_of(p.solve) == h->mode && p.thermal == h->thermal &&
+           p.precision == h->precision;
+}
+
+// Claim a scene slot and its cell range; walls are reserved with wall_cap entries.
+int32_t open_scene(SphHandle* h, const SphParams& p, int64_t wall_cap, int64_t first_step, int64_t last_step,
+                   int* out) {
+    int s = -1;
+    for (int k = 0; k < h->scap; ++k)
+        if (!h->scenes[k].used) {
+            s = k;
+            break;
+        }
+    if (s < 0) return fail(h, SPH_ERR_OOM, "no free scene slot");
+    SceneDev S;
+    std::string err;
+    if (!build_scene(p, S, err)) return fail(h, SPH_ERR_ARG, err);
+    const int64_t span = (int64_t)S.ncells + 1;
+    int64_t coff = 0, woff = 0;
+    if (!h->cells.alloc(span, &coff)) return fail(h, SPH_ERR_OOM, "cell capacity exhausted");
+    if (!h->walls.alloc(wall_cap, &woff)) {
+        h->cells.release(coff, span);
+        return fail(h, SPH_ERR_OOM, "wall capacity exhausted");
+    }
+    S.cell_off = (int32_t)coff;
+    S.last_step = last_step;
+    S.active = 1;
+    SceneRec& R = h->scenes[s];
+    R = SceneRec();
+    R.used = true;
+    R.dev = S;
+    R.cell_span = (int32_t)span;
+    R.wall_off = woff;
+    R.wall_cap = wall_cap;
+    R.first_step = first_step;
+    int32_t rc = upload_scene_const(h, s);
+    if (rc == SPH_OK) rc = set_scene_step(h, s, first_step);
+    if (rc == SPH_OK) rc = write_scene_walls(h, s);  // empty cell starts
+    if (rc != SPH_OK) return rc;
+    *out = s;
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sph_version(void) { return SPH_ABI_VERSION; }
+
+int32_t sph_create(const SphParams* params, int64_t fluid_capacity, int64_t wall_capacity, SphHandle** out) {
+    if (!params || !out) return fail(nullptr, SPH_ERR_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(nullptr, SPH_ERR_NO_DEVICE, "no CUDA device");
+    if (fluid_capacity < 1 || fluid_capacity > (int64_t)INT32_MAX / 8 || wall_capacity < 0 ||
+        wall_capacity > (int64_t)INT32_MAX / 2)
+        return fail(nullptr, SPH_ERR_ARG, "capacity out of range");
+    SceneDev S;
+    std::string err;
+    if (!build_scene(*params, S, err)) return fail(nullptr, SPH_ERR_ARG, err);
+    SphHandle* h = new SphHandle();
+    h->prm = *params;
+    h->dim = params->dim;
+    h->kernel = params->kernel;
+    h->mode = mode_of(params->solve);
+    h->thermal = params->thermal;
+    h->precision = params->precision;
+    h->cap = fluid_capacity;
+    h->wcap = wall_capacity;
+    h->scap = 1;
+    int32_t rc = allocate_handle(h, (int64_t)S.ncells + 1);
+    int s = 0;
+    if (rc == SPH_OK) rc = open_scene(h, *params, wall_capacity, 1, INT64_MAX, &s);
+    if (rc != SPH_OK) {
+        if (h->err.size()) g_create_error = h->err;
+        sph_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return SPH_OK;
+}
+
+int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double* v, const double* rho,
+                         const double* p, const double* c, const double* mass, const double* gap, const double* t,
+                         const double* kappa, const double* cp) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles take fluid through sph_batch_add_scene");
+    if (n < 0 || n > h->cap) return fail(h, SPH_ERR_GRID_OVERFLOW, "fluid count exceeds the handle capacity");
+    SceneRec& R = h->scenes[0];
+    bool uniform = true;
+    for (int64_t i = 1; i < n; ++i) uniform &= gap[i] == gap[0];
+    R.dev.uniform_gap = uniform ? 1 : 0;
+    int32_t rc = upload_scene_const(h, 0);
+    if (rc != SPH_OK) return rc;
+    rc = append_fluid(h, 0, 0, n, x, v, rho, p, c, mass, gap, t, kappa, cp);  // replaces the state
+    if (rc != SPH_OK) return rc;
+    h->have_fluid = true;
+    return SPH_OK;
+}
+
+int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x, const double* normal,
+                         const double* gap, const double* t, const double* kappa, const double* v) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles take walls through sph_batch_add_scene");
+    SceneRec& R = h->scenes[0];
+    if ((int64_t)R.wgap.size() + n > R.wall_cap) return fail(h, SPH_ERR_GRID_OVERFLOW, "wall count exceeds the handle capacity");
+    int32_t rc = add_walls_host(h, R, kind, n, x, normal, gap, t, kappa, v);
+    if (rc != SPH_OK) return rc;
+    return write_scene_walls(h, 0);
+}
+
+int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles step with sph_batch_step");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_step before sph_upload_fluid");
+    if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
+    if (nsteps == 0) return SPH_OK;
+    if (first_step != h->scenes[0].step_host) {  // the device counter only needs a reset on a jump
+        int32_t rc = set_scene_step(h, 0, first_step);
+        if (rc != SPH_OK) return rc;
+    }
+    return step_all_async(h, nsteps);
 }
 
 int32_t sph_synchronize(SphHandle* h) {
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     cudaStream_t st = h->stream;
-    SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned_step[1], h->sc.status, 4, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned[1], h->sc.status, 4, cudaMemcpyDeviceToHost, st));
     SPH_CUDA(h, cudaMemsetAsync(h->sc.status, 0, 4, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));
     int32_t status = 0;
-    std::memcpy(&status, &h->h_pinned_step[1], 4);
-    if ((status & kStatusNonFinite) && h->prm.nan_check)
+    std::memcpy(&status, &h->h_pinned[1], 4);
+    bool nan_check = h->prm.nan_check;
+    for (const SceneRec& R : h->scenes) nan_check |= R.used && R.dev.nan_check;
+    if ((status & kStatusNonFinite) && nan_check)
         return fail(h, SPH_ERR_NAN, "non-finite fluid state (density, velocity or position)");
     return SPH_OK;
 }
@@ -679,71 +915,170 @@ int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, doubl
                            double* p, double* c, double* mass, double* gap, double* t, double* kappa, double* cp) {
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!n_out) return fail(h, SPH_ERR_ARG, "n_out is required");
-    cudaStream_t st = h->stream;
-    int32_t n32 = 0;
-    SPH_CUDA(h, cudaMemcpyAsync(&n32, h->nbuf + h->par, 4, cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    const int64_t n = h->have_fluid ? n32 : 0;
-    *n_out = n;
-    if (n > capacity) return fail(h, SPH_ERR_ARG, "caller arrays too small for the live fluid");
-    if (n == 0) return SPH_OK;
-    const int dim = h->dim;
-    const SortedState& s = h->S[h->par];
-    const size_t vb = vec_bytes(dim);
-    std::vector<int32_t> ids(n);
-    SPH_CUDA(h, cudaMemcpyAsync(ids.data(), s.id, n * 4, cudaMemcpyDeviceToHost, st));
-    std::vector<char> bx, bv;
-    std::vector<double> b1[8];
-    const double* srcs[8] = {s.rho, s.p, s.c, s.m, s.gap, s.T, s.kappa, s.cp};
-    double* dsts[8] = {rho, p, c, mass, gap, t, kappa, cp};
-    if (x) {
-        bx.resize(n * vb);
-        SPH_CUDA(h, cudaMemcpyAsync(bx.data(), s.x, n * vb, cudaMemcpyDeviceToHost, st));
+    if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles download with sph_batch_download_scene");
+    if (!h->have_fluid) {
+        *n_out = 0;
+        return SPH_OK;
     }
-    if (v) {
-        bv.resize(n * vb);
-        SPH_CUDA(h, cudaMemcpyAsync(bv.data(), s.v, n * vb, cudaMemcpyDeviceToHost, st));
-    }
-    for (int f = 0; f < 8; ++f) {
-        if (!dsts[f] || !srcs[f]) continue;
-        b1[f].resize(n);
-        SPH_CUDA(h, cudaMemcpyAsync(b1[f].data(), srcs[f], n * 8, cudaMemcpyDeviceToHost, st));
-    }
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    // ascending id = the caller's original order with deleted particles removed
-    std::vector<int64_t> order(n);
-    for (int64_t k = 0; k < n; ++k) order[k] = k;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return ids[a] < ids[b]; });
-    for (int64_t q = 0; q < n; ++q) {
-        const int64_t k = order[q];
-        for (int d = 0; d < dim; ++d) {
-            if (x) x[q * dim + d] = ((const double*)(bx.data() + k * vb))[d];
-            if (v) v[q * dim + d] = ((const double*)(bv.data() + k * vb))[d];
-        }
-        for (int f = 0; f < 8; ++f)
-            if (dsts[f] && srcs[f]) dsts[f][q] = b1[f][k];
-    }
-    return SPH_OK;
+    return download_scene(h, 0, capacity, n_out, x, v, rho, p, c, mass, gap, t, kappa, cp, nullptr);
 }
 
 int32_t sph_download_ids(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* ids_out) {
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!n_out) return fail(h, SPH_ERR_ARG, "n_out is required");
-    cudaStream_t st = h->stream;
-    int32_t n32 = 0;
-    SPH_CUDA(h, cudaMemcpyAsync(&n32, h->nbuf + h->par, 4, cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    const int64_t n = h->have_fluid ? n32 : 0;
-    *n_out = n;
-    if (n > capacity) return fail(h, SPH_ERR_ARG, "caller array too small for the live fluid");
-    if (n == 0 || !ids_out) return SPH_OK;
-    std::vector<int32_t> ids(n);
-    SPH_CUDA(h, cudaMemcpyAsync(ids.data(), h->S[h->par].id, n * 4, cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    std::sort(ids.begin(), ids.end());
-    for (int64_t k = 0; k < n; ++k) ids_out[k] = ids[k];
+    if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles download with sph_batch_download_scene");
+    if (!h->have_fluid) {
+        *n_out = 0;
+        return SPH_OK;
+    }
+    return download_scene(h, 0, capacity, n_out, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                          nullptr, nullptr, nullptr, ids_out);
+}
+
+// ------------------------------------------------------------------ batch / serving
+int32_t sph_batch_create(const SphParams* prototype, int64_t particle_capacity, int64_t cell_capacity,
+                         int64_t wall_capacity, int32_t scene_capacity, SphHandle** out) {
+    if (!prototype || !out) return fail(nullptr, SPH_ERR_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return fail(nullptr, SPH_ERR_NO_DEVICE, "no CUDA device");
+    if (particle_capacity < 1 || particle_capacity > (int64_t)INT32_MAX / 8 || cell_capacity < 2 ||
+        cell_capacity > (int64_t)scan_max_cells() || wall_capacity < 0 || wall_capacity > (int64_t)INT32_MAX / 2 ||
+        scene_capacity < 1 || scene_capacity > (1 << 20))
+        return fail(nullptr, SPH_ERR_ARG, "capacity out of range");
+    SceneDev S;
+    std::string err;
+    if (!build_scene(*prototype, S, err)) return fail(nullptr, SPH_ERR_ARG, err);
+    SphHandle* h = new SphHandle();
+    h->batch = true;
+    h->prm = *prototype;
+    h->dim = prototype->dim;
+    h->kernel = prototype->kernel;
+    h->mode = mode_of(prototype->solve);
+    h->thermal = prototype->thermal;
+    h->precision = prototype->precision;
+    h->cap = particle_capacity;
+    h->wcap = wall_capacity;
+    h->scap = scene_capacity;
+    int32_t rc = allocate_handle(h, cell_capacity);
+    if (rc != SPH_OK) {
+        sph_destroy(h);
+        return rc;
+    }
+    h->have_fluid = true;
+    *out = h;
     return SPH_OK;
 }
+
+int32_t sph_batch_add_scene(SphHandle* h, const SphParams* params, int64_t first_step, int64_t nsteps, int64_t n,
+                            const double* x, const double* v, const double* rho, const double* p, const double* c,
+                            const double* mass, const double* gap, const double* t, const double* kappa,
+                            const double* cp, int64_t n_wall, const int32_t* wall_kind, const double* wall_x,
+                            const double* wall_normal, const double* wall_gap, const double* wall_t,
+                            const double* wall_kappa, const double* wall_v, int32_t* scene_id) {
+    if (!h || !params || !scene_id) return fail(h, SPH_ERR_ARG, "null argument");
+    if (!h->batch) return fail(h, SPH_ERR_STATE, "not a batch handle");
+    if (!same_kind(h, *params)) return fail(h, SPH_ERR_ARG, "scene differs from the batch in dim/kernel/solve/form");
+    if (n < 0 || n_wall < 0 || nsteps < 0) return fail(h, SPH_ERR_ARG, "negative count");
+    if (n_wall > 0 && !wall_kind) return fail(h, SPH_ERR_ARG, "wall kinds are required");
+    int32_t n_before = 0;
+    int32_t rc = read_live(h, &n_before);
+    if (rc != SPH_OK) return rc;
+    if ((int64_t)n_before + n > h->cap) return fail(h, SPH_ERR_OOM, "particle capacity exhausted");
+    int s = -1;
+    rc = open_scene(h, *params, n_wall, first_step, first_step + nsteps - 1, &s);
+    if (rc != SPH_OK) return rc;
+    SceneRec& R = h->scenes[s];
+    const int dim = h->dim;
+    for (int64_t w = 0; w < n_wall && rc == SPH_OK; ++w)
+        rc = add_walls_host(h, R, wall_kind[w], 1, wall_x + w * dim, wall_normal + w * dim, wall_gap + w,
+                            wall_t ? wall_t + w : nullptr, wall_kappa ? wall_kappa + w : nullptr,
+                            wall_v ? wall_v + w * dim : nullptr);
+    bool uniform = true;
+    for (int64_t i = 1; i < n; ++i) uniform &= gap[i] == gap[0];
+    R.dev.uniform_gap = uniform ? 1 : 0;
+    if (rc == SPH_OK) rc = upload_scene_const(h, s);
+    if (rc == SPH_OK) rc = write_scene_walls(h, s);
+    if (rc == SPH_OK) rc = append_fluid(h, s, n_before, n, x, v, rho, p, c, mass, gap, t, kappa, cp);
+    if (rc != SPH_OK) {
+        const std::string keep = h->err;
+        R.dev.active = 0;
+        upload_scene_const(h, s);
+        h->cells.release(R.dev.cell_off, R.cell_span);
+        h->walls.release(R.wall_off, R.wall_cap);
+        R = SceneRec();
+        h->err = keep;
+        return rc;
+    }
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);  // Shepard patterns change
+    h->graphs.clear();
+    *scene_id = s;
+    return SPH_OK;
+}
+
+int32_t sph_batch_step(SphHandle* h, int64_t nsteps) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->batch) return fail(h, SPH_ERR_STATE, "not a batch handle");
+    if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
+    if (nsteps == 0) return SPH_OK;
+    return step_all_async(h, nsteps);
+}
+
+int32_t sph_batch_scene_info(SphHandle* h, int32_t scene_id, int64_t* info) {
+    if (!h || !info) return fail(h, SPH_ERR_ARG, "null argument");
+    if (scene_id < 0 || scene_id >= h->scap || !h->scenes[scene_id].used) return fail(h, SPH_ERR_ARG, "no such scene");
+    const SceneRec& R = h->scenes[scene_id];
+    int32_t b = 0, e = 0;
+    int32_t rc = scene_range(h, scene_id, &b, &e);
+    if (rc != SPH_OK) return rc;
+    const int64_t total = R.dev.last_step - R.first_step + 1;
+    const int64_t done = std::min<int64_t>(R.step_host - R.first_step, total);
+    info[0] = e - b;
+    info[1] = done;
+    info[2] = done >= total ? 1 : 0;
+    info[3] = R.step_host;
+    return SPH_OK;
+}
+
+int32_t sph_batch_download_scene(SphHandle* h, int32_t scene_id, int64_t capacity, int64_t* n_out, double* x,
+                                 double* v, double* rho, double* p, double* c, double* mass, double* gap, double* t,
+                                 double* kappa, double* cp) {
+    if (!h || !n_out) return fail(h, SPH_ERR_ARG, "null argument");
+    if (scene_id < 0 || scene_id >= h->scap || !h->scenes[scene_id].used) return fail(h, SPH_ERR_ARG, "no such scene");
+    return download_scene(h, scene_id, capacity, n_out, x, v, rho, p, c, mass, gap, t, kappa, cp, nullptr);
+}
+
+int32_t sph_batch_retire(SphHandle* h, int32_t scene_id) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->batch) return fail(h, SPH_ERR_STATE, "not a batch handle");
+    if (scene_id < 0 || scene_id >= h->scap || !h->scenes[scene_id].used) return fail(h, SPH_ERR_ARG, "no such scene");
+    SceneRec& R = h->scenes[scene_id];
+    R.dev.active = 0;
+    int32_t rc = upload_scene_const(h, scene_id);
+    if (rc == SPH_OK) rc = resort(h);  // drops the scene's particles
+    if (rc != SPH_OK) return rc;
+    h->cells.release(R.dev.cell_off, R.cell_span);
+    h->walls.release(R.wall_off, R.wall_cap);
+    R = SceneRec();
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return SPH_OK;
+}
+
+int32_t sph_batch_free(SphHandle* h, int64_t* out) {
+    if (!h || !out) return fail(h, SPH_ERR_ARG, "null argument");
+    int32_t n = 0;
+    int32_t rc = read_live(h, &n);
+    if (rc != SPH_OK) return rc;
+    int64_t slots = 0;
+    for (const SceneRec& R : h->scenes) slots += !R.used;
+    out[0] = h->cap - n;
+    out[1] = h->cells.largest();
+    out[2] = h->walls.largest();
+    out[3] = slots;
+    return SPH_OK;
+}
+
 
 int32_t sph_stats(SphHandle* h, SphStats* out) {
     if (!h || !out) return fail(h, SPH_ERR_ARG, "null argument");
@@ -759,7 +1094,8 @@ int32_t sph_stats(SphHandle* h, SphStats* out) {
     SPH_CUDA(h, cudaMemcpyAsync(&status, h->sc.status, 4, cudaMemcpyDeviceToHost, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));
     out->n_fluid = h->have_fluid ? n32 : 0;
-    out->n_wall = h->W.n;
+    out->n_wall = 0;
+    for (const SceneRec& R : h->scenes) out->n_wall += R.used ? R.wall_n : 0;
     out->steps_done = h->steps_done;
     out->total_mass = r[0];
     out->kinetic_energy = r[1];
@@ -928,7 +1264,7 @@ int32_t sph_destroy(SphHandle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : h->allocs) cudaFree(p);
-    if (h->h_pinned_step) cudaFreeHost(h->h_pinned_step);
+    if (h->h_pinned) cudaFreeHost(h->h_pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPH_OK;

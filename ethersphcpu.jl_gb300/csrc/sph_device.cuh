@@ -61,6 +61,9 @@ struct SceneDev {
     double dtdt;     // dt * dt
     int64_t reinit_interval;
     int64_t check_interval;
+    int64_t last_step;  // the scene is frozen (state kept, no physics) after this step
+    int32_t active;     // 0: retired, its particles are dropped at the next sort
+    int32_t pad_active;
     double check_lo[3];
     double check_hi[3];
     double two_pi_unused;

@@ -156,12 +156,14 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 
 // -------------------------------------------------------------------- K4 (FP32)
 template <int DIM, int KK, int TPP>
-__global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st,
-                                 const int32_t* __restrict__ start, const int32_t* __restrict__ n_live, int32_t cap) {
+__global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
-    if (i >= cap || i >= *n_live) return;
-    const SceneDev& S = scenes[st.scene[i]];
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    if (!scene_runs(S, sc.scene_step[s])) return;
+    const int32_t* __restrict__ start = sc.start;
     const float4 ai = st.fa[i];
     float xi[3], vi[3];
     if (DIM == 2) {
@@ -236,6 +238,10 @@ __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState 
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
+    if (!scene_runs(S, sc.scene_step[s])) {
+        if (lane == 0) carry_frozen<DIM>(i, S, st, nx, sc);
+        return;
+    }
     const float4 ai = st.fa[i];
     const float4 bi = st.fb[i];
     float xi[3], vi[3], m_i, rho_i, P_i, gap_i;
@@ -472,7 +478,8 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
-    if (!force && !is_step(sc.scene_step[s], S.reinit_interval)) return;
+    const int64_t step_s = sc.scene_step[s];
+    if (!scene_runs(S, step_s) || (!force && !is_step(step_s, S.reinit_interval))) return;
     const float4 ai = st.fa[i];
     const float xi0 = ai.x, xi1 = ai.y, xi2 = DIM == 3 ? ai.z : 0.f;
     int32_t c[3];
@@ -504,7 +511,7 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        k_continuity_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+        k_continuity_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
     } else if (stage == 2) {
         k_reinit_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap, L.force_reinit);
     } else if (mode == kModeFluidWall) {

@@ -25,12 +25,14 @@ enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2 };
 
 template <int DIM, int KK>
 __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restrict__ scenes, SortedState st,
-                                                         const int32_t* __restrict__ start,
-                                                         const int32_t* __restrict__ n_live, int32_t cap) {
+                                                         SortScratch sc, int32_t cap) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cap || i >= *n_live) return;
-    const SceneDev& S = scenes[st.scene[i]];
+    if (i >= cap || i >= *sc.n_live) return;
+    const int32_t s = st.scene[i];
+    const SceneDev& S = scenes[s];
+    if (!scene_runs(S, sc.scene_step[s])) return;
+    const int32_t* __restrict__ start = sc.start;
     const V* __restrict__ x = (const V*)st.x;
     const V* __restrict__ v = (const V*)st.v;
     const V xi = x[i];
@@ -80,6 +82,10 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
     const int64_t step = sc.scene_step[s];
+    if (!scene_runs(S, step)) {
+        carry_frozen<DIM>(i, S, st, nx, sc);
+        return;
+    }
     const V* __restrict__ x = (const V*)st.x;
     const V* __restrict__ v = (const V*)st.v;
     const V xi = x[i];
@@ -291,7 +297,8 @@ __global__ void __launch_bounds__(128) k_reinit_fp64(const SceneDev* __restrict_
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
-    if (!force && !is_step(sc.scene_step[s], S.reinit_interval)) return;
+    const int64_t step = sc.scene_step[s];
+    if (!scene_runs(S, step) || (!force && !is_step(step, S.reinit_interval))) return;
     const V* __restrict__ x = (const V*)st.x;
     const V xi = x[i];
     int32_t c[3];
@@ -321,7 +328,7 @@ namespace {
 template <int DIM, int KK>
 void launch_k4(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
-    k_continuity_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc.start, L.sc.n_live, L.cap);
+    k_continuity_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
 }
 template <int DIM, int KK, int MODE>
 void launch_k5(const LaunchCtx& L) {

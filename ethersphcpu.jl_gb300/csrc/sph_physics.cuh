@@ -209,4 +209,28 @@ __device__ __forceinline__ bool is_step(int64_t step, int64_t interval) {
     return interval > 0 && step % interval == 0;
 }
 
+// A scene takes part in the physics of a step while it is active and has steps left.
+__device__ __forceinline__ bool scene_runs(const SceneDev& S, int64_t step) { return S.active && step <= S.last_step; }
+
+// The momentum kernel's work for a particle of a scene that does not run this step:
+// carry the state unchanged into the step outputs and hash it for the next sort (or
+// drop it when the scene was retired).
+template <int DIM>
+__device__ __forceinline__ void carry_frozen(int i, const SceneDev& S, const SortedState& st, const NextState& nx,
+                                             const SortScratch& sc) {
+    using V = typename VecT<DIM>::T;
+    if (!S.active) {
+        sc.key[i] = kDeadKey;
+        return;
+    }
+    const V x = ((const V*)st.x)[i];
+    ((V*)nx.x)[i] = x;
+    ((V*)nx.v)[i] = ((const V*)st.v)[i];
+    nx.rho[i] = st.rho[i];
+    if (nx.T) nx.T[i] = st.T[i];
+    const int32_t key = cell_key<DIM>(x, S);
+    sc.key[i] = key;
+    sc.slot[i] = atomicAdd(sc.count + key, 1);
+}
+
 }  // namespace sph

@@ -33,6 +33,10 @@ __global__ void k_hash(const SceneDev* __restrict__ scenes, NextState nx, Sorted
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
     const SceneDev& S = scenes[st.scene[i]];
+    if (!S.active) {  // retired scene: dropped by this sort
+        sc.key[i] = kDeadKey;
+        return;
+    }
     const V x = ((const V*)nx.x)[i];
     const int32_t key = cell_key<DIM>(x, S);
     sc.key[i] = key;

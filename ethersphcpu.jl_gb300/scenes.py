@@ -331,3 +331,62 @@ def lid_driven_cavity_2d(n=100, reynolds=100.0, lid_velocity=1.0, reinit=100, to
     hi = (L + t * dr + rc, L + t * dr + rc)
     return Scene(name, fluid, [walls], kernel, model, td, _abi.SOLVE_FLUID_VELOCITY_WALL, None, lo, hi,
                  meta=dict(n=n, reynolds=reynolds, dx=dr))
+
+
+# ---------------------------------------------------------------- batched and served workloads
+def random_dam_break_2d(rng, dx=0.01, total_step=1000, kernel="CubicSpline", name="dam_break"):
+    """One scene of the batched distribution: column width W ~ U[0.3, 1.5] m, height/width
+    ~ U[0.5, 3], tank 4W x 1.5 H, the physics of dam_break_2d (c0 = 10 sqrt(2 g H))."""
+    W = float(rng.uniform(0.3, 1.5))
+    H = float(rng.uniform(0.5, 3.0)) * W
+    return dam_break_2d(dx=dx, water_w=W, water_h=H, box_w=4.0 * W, box_h=1.5 * H, total_step=total_step,
+                        kernel=kernel, name=name)
+
+
+def batched_dam_breaks(n_scenes=512, seed=0, dx=0.01, total_step=1000, kernel="CubicSpline"):
+    """The batched workload: n_scenes seeded 2D dam breaks (about 450 to 67,500 fluid
+    particles each) for one launch of the batch kernels."""
+    rng = np.random.default_rng(seed)
+    return [random_dam_break_2d(rng, dx, total_step, kernel, name=f"dam_break_{k}") for k in range(n_scenes)]
+
+
+def random_poiseuille_2d(rng, total_step=1000, kernel="CubicSpline", name="poiseuille"):
+    """Served Poiseuille channel: H = 1 mm, L = 4H, nu = 1e-6, Re ~ U[0.01, 1],
+    dx = H / U{20..80}, periodic in x."""
+    return poiseuille_periodic_2d(H=1e-3, length_factor=4.0, nu=1e-6, reynolds=float(rng.uniform(0.01, 1.0)),
+                                  n_across=int(rng.integers(20, 81)), total_step=total_step, kernel=kernel,
+                                  name=name)
+
+
+def random_dam_break_3d(rng, total_step=1000, kernel="WendlandC4", name="dam_break_3d"):
+    """Served 3D dam break: dx ~ U[0.01, 0.02] m, a 0.4 x 0.4 x 0.65 m column (about 13k
+    to 110k particles) in a 1.6 x 0.4 x 0.8 m tank."""
+    dx = float(rng.uniform(0.01, 0.02))
+    return dam_break_3d(dx=dx, tank=(1.6, 0.4, 0.8), column=(0.4, 0.4, 0.65), total_step=total_step, kernel=kernel,
+                        name=name)
+
+
+@dataclass
+class Request:
+    t_arrival: float
+    kind: str       # "dam_break_2d" | "poiseuille_2d" | "dam_break_3d"
+    nsteps: int
+    seed: int
+
+    def build(self):
+        rng = np.random.default_rng(self.seed)
+        if self.kind == "dam_break_2d":
+            return random_dam_break_2d(rng, total_step=self.nsteps, name=f"req{self.seed}")
+        if self.kind == "poiseuille_2d":
+            return random_poiseuille_2d(rng, total_step=self.nsteps, name=f"req{self.seed}")
+        return random_dam_break_3d(rng, total_step=self.nsteps, name=f"req{self.seed}")
+
+
+def poisson_stream(rate, count, seed=0, steps=(500, 5000), kinds=("dam_break_2d", "poiseuille_2d", "dam_break_3d")):
+    """A served request stream: Poisson arrivals at `rate` per second, kinds drawn with
+    equal probability, step budgets ~ U{steps[0]..steps[1]}."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    kind = rng.integers(0, len(kinds), count)
+    nsteps = rng.integers(steps[0], steps[1] + 1, count)
+    return [Request(float(t[k]), kinds[int(kind[k])], int(nsteps[k]), seed * 1_000_003 + k) for k in range(count)]

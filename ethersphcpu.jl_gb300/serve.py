@@ -1,0 +1,131 @@
+"""Serving loop: scene requests arrive over time, stay resident on the device, are
+admitted by device-memory footprint, stepped together, retired when done.
+
+This is continuous batching, not a queue: requests that arrive while others run are
+added to the running batch as soon as particle slots, a contiguous run of cells and of
+wall slots and a scene slot are free (sph_batch_free), every bundle of steps advances
+every resident scene in the same kernel launches, and finished scenes are downloaded and
+retired between bundles, which frees their memory for the queue.  2D and 3D scenes use
+two batch handles (the kernels are specialised by dimension); each has its own CUDA
+stream, so their bundles overlap on the GPU.
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .batch import Batch, bytes_per, footprint
+
+
+@dataclass
+class Completed:
+    request: object
+    t_admit: float
+    t_done: float
+    n_fluid: int
+    result: dict = field(repr=False, default=None)
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.request.t_arrival
+
+
+@dataclass
+class Report:
+    completed: list
+    wall_s: float
+    particle_steps: int
+
+    def summary(self) -> dict:
+        lat = np.array([c.latency for c in self.completed]) if self.completed else np.zeros(1)
+        return {
+            "requests": len(self.completed),
+            "wall_s": self.wall_s,
+            "particle_steps": self.particle_steps,
+            "particle_steps_per_s": self.particle_steps / self.wall_s if self.wall_s > 0 else 0.0,
+            "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)),
+            "latency_mean_s": float(lat.mean()),
+        }
+
+
+class Server:
+    def __init__(self, budget_bytes: float = 150e9, precision: int = _abi.PRECISION_FP32_COMPENSATED,
+                 share_3d: float = 0.4, bundle: int = 10, scene_capacity: int = 4096, keep_results: bool = False,
+                 launch_shape=None, lib=None):
+        from . import scenes
+        self.bundle = bundle
+        self.precision = precision
+        self.keep_results = keep_results
+        proto2 = scenes.dam_break_2d(dx=0.05).params(precision=precision)
+        proto3 = scenes.dam_break_3d(dx=0.05, tank=(0.4, 0.2, 0.4), column=(0.1, 0.1, 0.2)).params(precision=precision)
+        self.batches = {
+            2: Batch.for_budget(proto2, int(budget_bytes * (1.0 - share_3d)), scene_capacity,
+                                cells_per_particle=3.0, walls_per_particle=0.6, lib=lib),
+            3: Batch.for_budget(proto3, int(budget_bytes * share_3d), scene_capacity,
+                                cells_per_particle=2.0, walls_per_particle=3.0, lib=lib),
+        }
+        if launch_shape is not None:
+            for b in self.batches.values():
+                b.set_launch_shape(*launch_shape)
+
+    def close(self):
+        for b in self.batches.values():
+            b.close()
+
+    def run(self, requests, time_limit: float | None = None) -> Report:
+        pending = collections.deque(sorted(requests, key=lambda r: r.t_arrival))
+        queues = {2: collections.deque(), 3: collections.deque()}
+        active = {}  # (dim, sid) -> [request, t_admit, steps_left, n_fluid]
+        done = []
+        particle_steps = 0
+        t0 = time.perf_counter()
+        while pending or active or any(queues.values()):
+            now = time.perf_counter() - t0
+            if time_limit is not None and now > time_limit:
+                break
+            while pending and pending[0].t_arrival <= now:
+                r = pending.popleft()
+                scene = r.build()
+                queues[scene.kernel.dim_].append((r, scene))
+            # admission: first come first served per dimension, while the footprint fits
+            for dim, q in queues.items():
+                b = self.batches[dim]
+                while q:
+                    r, scene = q[0]
+                    p, c, w = footprint(scene)
+                    fr = b.free()
+                    if not (p <= fr["particles"] and c <= fr["cells"] and w <= fr["walls"] and fr["scenes"] >= 1):
+                        break
+                    q.popleft()
+                    sid = b.add_scene(scene, first_step=1, nsteps=r.nsteps)
+                    active[(dim, sid)] = [r, time.perf_counter() - t0, r.nsteps, scene.n_fluid]
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, min(0.01, pending[0].t_arrival - (time.perf_counter() - t0))))
+                continue
+            # one bundle of steps for every resident scene (both batches, overlapping)
+            running = {dim for (dim, _sid) in active}
+            for dim in running:
+                self.batches[dim].step(self.bundle)
+            for dim in running:
+                self.batches[dim].synchronize()
+            t_now = time.perf_counter() - t0
+            for key in list(active):
+                rec = active[key]
+                steps = min(self.bundle, rec[2])
+                particle_steps += steps * rec[3]
+                rec[2] -= steps
+                if rec[2] <= 0:
+                    dim, sid = key
+                    b = self.batches[dim]
+                    result = b.download(sid) if self.keep_results else None
+                    n_end = b.info(sid)["n_fluid"] if not self.keep_results else len(result["rho"])
+                    b.retire(sid)
+                    done.append(Completed(rec[0], rec[1], t_now, n_end, result))
+                    del active[key]
+        return Report(done, time.perf_counter() - t0, particle_steps)

@@ -226,6 +226,51 @@ enum {
 };
 int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out);
 
+/* ---- batched scenes and serving ---------------------------------------------------
+ * A batch handle steps many independent scenes (same dim, kernel, solve variant, form
+ * and thermal flag; any geometry, resolution and physical constants) in the same kernel
+ * launches: particles of all scenes share the sorted arrays, every scene owns a range
+ * of cells and a region of the wall arrays, and every scene advances its own step
+ * counter (Shepard and check steps follow each scene's own step numbers).  Capacities
+ * are fixed at creation (that is the device memory budget); scenes can be added and
+ * retired between steps, so requests are served while others run.  No reference
+ * counterpart: EtherSPHCPU.jl runs one solve! per process. */
+
+/* prototype: dim, kernel, solve, precision and thermal of every scene of the batch. */
+int32_t sph_batch_create(const SphParams* prototype, int64_t particle_capacity, int64_t cell_capacity,
+                         int64_t wall_capacity, int32_t scene_capacity, SphHandle** out);
+
+/* Add a scene that will run steps first_step .. first_step+nsteps-1 and then stay
+ * frozen (state kept) until retired.  Fluid arrays as in sph_upload_fluid; walls as one
+ * merged set with a kind per particle (wall_t/wall_kappa read for thermostatic walls,
+ * wall_v for static-velocity walls; may be NULL otherwise).  SPH_ERR_OOM when a
+ * capacity (particles, a contiguous run of cells or walls, scene slots) is exhausted. */
+int32_t sph_batch_add_scene(SphHandle* h, const SphParams* params, int64_t first_step, int64_t nsteps, int64_t n,
+                            const double* x, const double* v, const double* rho, const double* p, const double* c,
+                            const double* mass, const double* gap, const double* t, const double* kappa,
+                            const double* cp, int64_t n_wall, const int32_t* wall_kind, const double* wall_x,
+                            const double* wall_normal, const double* wall_gap, const double* wall_t,
+                            const double* wall_kappa, const double* wall_v, int32_t* scene_id);
+
+/* Run nsteps steps of every scene (frozen scenes are carried unchanged); asynchronous,
+ * sph_synchronize() waits and reports non-finite states. */
+int32_t sph_batch_step(SphHandle* h, int64_t nsteps);
+
+/* info[4] = (live particles, steps done, finished (0/1), next step number). */
+int32_t sph_batch_scene_info(SphHandle* h, int32_t scene_id, int64_t* info);
+
+/* Live particles of one scene in their original order (as sph_download_fluid). */
+int32_t sph_batch_download_scene(SphHandle* h, int32_t scene_id, int64_t capacity, int64_t* n_out, double* x,
+                                 double* v, double* rho, double* p, double* c, double* mass, double* gap, double* t,
+                                 double* kappa, double* cp);
+
+/* Drop a scene's particles and free its slot, cells and walls. */
+int32_t sph_batch_retire(SphHandle* h, int32_t scene_id);
+
+/* out[4] = (free particle slots, largest free run of cells, largest free run of walls,
+ * free scene slots): what admission control compares a scene's footprint with. */
+int32_t sph_batch_free(SphHandle* h, int64_t* out);
+
 /* Pair counting that allocates no device memory.  No counterpart in the reference:
  * it serves callers that cannot let a library call cudaMalloc or cudaFree (device
  * memory owned by another framework's stream-ordered pool, code that must not cause
