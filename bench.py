@@ -49,6 +49,11 @@ def parse():
     ap.add_argument("--n", type=int, default=256, help="cavity resolution (n x n fluid particles)")
     ap.add_argument("--cpu-sample-steps", type=int, default=0, help="CPU baseline steps (0: auto, ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-scene batched workload")
+    ap.add_argument("--no-served", action="store_true", help="skip the served Poisson stream")
+    ap.add_argument("--batched-steps", type=int, default=20)
+    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-rate", type=float, default=100.0)
     ap.add_argument("--only-steps", action="store_true",
                     help="upload, warm up and run the timed steps only (the command profiled with ncu)")
     return ap.parse_args()
@@ -353,6 +358,74 @@ def run_ours(args, rank, world, local):
     return out
 
 
+def time_batch_steps(bt, steps, warmup):
+    """CUDA-event time of `steps` steps of a batch (its state is larger than L2)."""
+    import torch
+    stream = torch.cuda.ExternalStream(bt.stream())
+    for _ in range(warmup):
+        bt.step(1)
+    bt.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    bt.step(steps)
+    e1.record(stream)
+    bt.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_batched(args):
+    """512 seeded 2D dam breaks (dx 0.01, 450-67,500 fluid particles each) stepped in one
+    set of launches: FP32-compensated with an autotuned launch shape, and plain FP64."""
+    import ethersph_gb300  # noqa: F401
+    from ethersph_gb300 import batch, scenes
+    sc = scenes.batched_dam_breaks(512, seed=0)
+    nf = sum(s.n_fluid for s in sc)
+    nw = sum(s.n_wall for s in sc)
+    nc = sum(batch.footprint(s)[1] for s in sc)
+    res = {"workload": f"512 batched 2D dam breaks, {nf} fluid + {nw} wall particles, {nc} cells, CubicSpline, "
+                       "FluidWallSolve, per-scene c0 and dt", "fluid_particles": nf,
+           "l2": "state larger than L2 (no flush)"}
+    for prec, steps in ((1, args.batched_steps), (0, 2)):
+        with batch.Batch(sc[0].params(precision=prec), nf + 1024, nc + 1024, nw + 1024, 512) as bt:
+            for s in sc:
+                bt.add_scene(s, 1, 1000)
+            shape = bt.autotune(2) if prec == 1 else None
+            ms = time_batch_steps(bt, steps, 2)
+            key = "fp32c" if prec == 1 else "fp64"
+            res[key] = {"ms_per_step": ms, "particle_steps_per_s": nf / (ms / 1e3), "steps": steps}
+            if shape:
+                res[key]["launch_shape"] = shape
+                res[key]["stages_ms"] = bt.time_stages(3)
+    res["fp32c_over_fp64"] = res["fp32c"]["particle_steps_per_s"] / res["fp64"]["particle_steps_per_s"]
+    return res
+
+
+def run_served(args):
+    """A Poisson stream of mixed scene requests (2D dam breaks, periodic 2D Poiseuille,
+    3D dam breaks) served by continuous batching; latency p50/p99 and particle-steps/s,
+    FP32-compensated vs plain FP64 on the same stream (shorter step budgets for FP64)."""
+    import ethersph_gb300  # noqa: F401
+    from ethersph_gb300 import scenes, serve
+    out = {}
+    for prec, count, steps in ((1, args.served_requests, (500, 5000)), (0, max(6, args.served_requests // 8),
+                                                                          (100, 400))):
+        reqs = scenes.poisson_stream(rate=args.served_rate, count=count, seed=0, steps=steps)
+        srv = serve.Server(budget_bytes=150e9 if prec == 1 else 40e9, precision=prec)
+        try:
+            rep = srv.run(reqs)
+        finally:
+            srv.close()
+        s = rep.summary()
+        s["rate_per_s"] = args.served_rate
+        s["steps_per_request"] = list(steps)
+        out["fp32c" if prec == 1 else "fp64"] = s
+    out["workload"] = ("Poisson arrivals, 1/3 each 2D dam break (batched distribution), periodic 2D Poiseuille "
+                       "(H=1mm, Re~U[0.01,1], dx=H/U{20..80}), 3D dam break (dx~U[0.01,0.02]); "
+                       "150 GB device budget (FP64: 40 GB)")
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -386,6 +459,10 @@ def main():
         return
     out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:
+        if not args.no_batched:
+            out["batched"] = run_batched(args)
+        if not args.no_served:
+            out["served"] = run_served(args)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(workload(args.n), args)
         print(json.dumps(out))

@@ -14,6 +14,9 @@ import numpy as np
 
 from . import _abi
 
+MAX_CELLS = 4096 * 1024 * 16      # what one three-level scan covers
+MAX_PARTICLES = (2**31 - 1) // 8  # int32 indices with up to 8 lanes per particle
+
 
 def merged_walls(scene):
     """The scene's wall groups as one set with a kind per particle."""
@@ -86,9 +89,9 @@ class Batch:
         """Size a batch to a device memory budget."""
         bp, bc, bw = bytes_per(prototype.dim, bool(prototype.thermal), prototype.precision)
         unit = bp + cells_per_particle * bc + walls_per_particle * bw
-        n = int(budget_bytes / unit)
-        return cls(prototype, n, max(2, int(n * cells_per_particle)), int(n * walls_per_particle),
-                   scene_capacity, lib=lib)
+        n = min(int(budget_bytes / unit), MAX_PARTICLES)
+        cells = max(2, min(int(n * cells_per_particle), MAX_CELLS))
+        return cls(prototype, n, cells, int(n * walls_per_particle), scene_capacity, lib=lib)
 
     def close(self):
         if self.h:

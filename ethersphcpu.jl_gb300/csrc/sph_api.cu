@@ -261,7 +261,8 @@ struct SphHandle {
     bool batch = false;
     int dim = 2, kernel = 0, mode = 0, thermal = 0, precision = 0;
     int64_t cap = 0, wcap = 0;
-    int32_t total_cells = 0;  // cell capacity (the scan covers all of it)
+    int32_t total_cells = 0;  // cell capacity
+    int32_t scan_cells = 1;   // end of the highest cell range in use: what the scan covers
     int32_t scap = 1;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
@@ -361,7 +362,7 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.thermal = h->thermal;
     L.precision = h->precision;
     L.cap = (int32_t)h->cap;
-    L.total_cells = h->total_cells;
+    L.total_cells = h->scan_cells;
     L.nscenes = h->scap;
     L.scenes = h->d_scenes;
     L.st = h->S[h->par];
@@ -405,7 +406,7 @@ int resort(SphHandle* h) {
     L.nx.v = L.st.v;
     L.nx.rho = L.st.rho;
     L.nx.T = L.st.T;
-    SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, h->stream));
+    SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, h->stream));
     launch_hash(L);
     launch_scan(L, 0);
     launch_place(L);
@@ -770,6 +771,18 @@ bool same_kind(const SphHandle* h, const SphParams& p) {
            p.precision == h->precision;
 }
 
+// The scan and the count clears cover cells [0, end of the highest range in use).
+void update_scan_range(SphHandle* h) {
+    int64_t hi = 1;
+    for (const SceneRec& R : h->scenes)
+        if (R.used) hi = std::max<int64_t>(hi, (int64_t)R.dev.cell_off + R.cell_span);
+    if (hi != h->scan_cells) {  // the step graphs bake the scan length
+        for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+        h->graphs.clear();
+    }
+    h->scan_cells = (int32_t)hi;
+}
+
 // Claim a scene slot and its cell range; walls are reserved with wall_cap entries.
 int32_t open_scene(SphHandle* h, const SphParams& p, int64_t wall_cap, int64_t first_step, int64_t last_step,
                    int* out) {
@@ -801,6 +814,7 @@ int32_t open_scene(SphHandle* h, const SphParams& p, int64_t wall_cap, int64_t f
     R.wall_off = woff;
     R.wall_cap = wall_cap;
     R.first_step = first_step;
+    update_scan_range(h);
     int32_t rc = upload_scene_const(h, s);
     if (rc == SPH_OK) rc = set_scene_step(h, s, first_step);
     if (rc == SPH_OK) rc = write_scene_walls(h, s);  // empty cell starts
@@ -1007,6 +1021,7 @@ int32_t sph_batch_add_scene(SphHandle* h, const SphParams* params, int64_t first
         h->cells.release(R.dev.cell_off, R.cell_span);
         h->walls.release(R.wall_off, R.wall_cap);
         R = SceneRec();
+        update_scan_range(h);
         h->err = keep;
         return rc;
     }
@@ -1060,6 +1075,7 @@ int32_t sph_batch_retire(SphHandle* h, int32_t scene_id) {
     h->cells.release(R.dev.cell_off, R.cell_span);
     h->walls.release(R.wall_off, R.wall_cap);
     R = SceneRec();
+    update_scan_range(h);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
     return SPH_OK;
@@ -1145,7 +1161,7 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
     auto run = [&](int stage) {
         switch (stage) {
             case SPH_STAGE_CELL_COUNT:
-                cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st);
+                cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st);
                 launch_hash(Lh);
                 break;
             case SPH_STAGE_SCAN: launch_scan(Lh, 0); break;
@@ -1165,12 +1181,12 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
         SPH_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
         ms_out[stage] = (double)ms / reps;
         if (stage == SPH_STAGE_CELL_COUNT) {  // leave a consistent cell list for the later stages
-            SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
+            SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
             launch_hash(Lh);
         }
     }
     // the momentum stage left arrivals in count[]: the next step expects it zeroed
-    SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
+    SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
     // restore p and c (output-only fields) from the copy the placement stage wrote
     const size_t n = (size_t)h->cap;
     SPH_CUDA(h, cudaMemcpyAsync(h->S[par].p, h->S[par ^ 1].p, n * 8, cudaMemcpyDeviceToDevice, st));
@@ -1229,7 +1245,7 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         h->tune[3] = best_block[1];
         // restore what the timed launches touched: p and c, and the arrivals left in
         // count[]; every other field they wrote is rebuilt by the next step before use
-        SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
+        SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par].p, h->S[par ^ 1].p, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par].c, h->S[par ^ 1].c, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaGetLastError());
