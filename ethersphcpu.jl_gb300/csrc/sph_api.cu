@@ -263,6 +263,7 @@ struct SphHandle {
     int64_t cap = 0, wcap = 0;
     int32_t total_cells = 0;  // cell capacity
     int32_t scan_cells = 1;   // end of the highest cell range in use: what the scan covers
+    int64_t n_upper = 1;      // bound on the live particles (only deletions change it while stepping)
     int32_t scap = 1;
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
@@ -361,7 +362,9 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.mode = h->mode;
     L.thermal = h->thermal;
     L.precision = h->precision;
-    L.cap = (int32_t)h->cap;
+    // per-particle grids cover the live bound, not the capacity (a served batch is sized
+    // for its memory budget and may hold far fewer particles)
+    L.cap = (int32_t)std::max<int64_t>(1, std::min<int64_t>(h->cap, h->n_upper));
     L.total_cells = h->scan_cells;
     L.nscenes = h->scap;
     L.scenes = h->d_scenes;
@@ -417,6 +420,15 @@ int resort(SphHandle* h) {
 }
 
 bool is_step_host(int64_t step, int64_t interval) { return interval > 0 && step % interval == 0; }
+
+// New bound on the live particles; the captured step graphs bake the grid sizes.
+void set_n_upper(SphHandle* h, int64_t n) {
+    if (n != h->n_upper) {
+        for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+        h->graphs.clear();
+    }
+    h->n_upper = n;
+}
 
 int32_t read_live(SphHandle* h, int32_t* n) {
     SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned[2], h->nbuf + h->par, 4, cudaMemcpyDeviceToHost, h->stream));
@@ -614,6 +626,7 @@ int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const dou
     }
     h->h_pinned[2] = 0;
     const int32_t total = (int32_t)(n_before + n);
+    set_n_upper(h, total);
     std::memcpy(&h->h_pinned[2], &total, 4);
     SPH_CUDA(h, cudaMemcpyAsync(h->nbuf + h->par, &h->h_pinned[2], 4, cudaMemcpyHostToDevice, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));  // host staging buffers die at return
@@ -1071,6 +1084,9 @@ int32_t sph_batch_retire(SphHandle* h, int32_t scene_id) {
     R.dev.active = 0;
     int32_t rc = upload_scene_const(h, scene_id);
     if (rc == SPH_OK) rc = resort(h);  // drops the scene's particles
+    int32_t n_left = 0;
+    if (rc == SPH_OK) rc = read_live(h, &n_left);
+    if (rc == SPH_OK) set_n_upper(h, n_left);
     if (rc != SPH_OK) return rc;
     h->cells.release(R.dev.cell_off, R.cell_span);
     h->walls.release(R.wall_off, R.wall_cap);
