@@ -181,14 +181,10 @@ def algorithmic_bytes(scene, precision):
     return nf * fluid + nw * wall
 
 
-def grid_cells(scene):
-    """Cells of the scene's grid (edge r_cut (1 + 1e-9), as the library builds it)."""
-    import math
-    edge = scene.kernel.influence_radius_ * (1.0 + 1e-9)
-    n = 1
-    for a in range(scene.kernel.dim_):
-        n *= max(1, math.ceil((scene.domain_hi[a] - scene.domain_lo[a]) / edge))
-    return n
+def grid_cells(scene, precision):
+    """Cells of the scene's grid, as the library builds it."""
+    from ethersph_gb300 import batch
+    return batch.grid_cells(scene, 0, precision)
 
 
 def time_form(pkg, _abi, scene, precision, steps, warmup, local):
@@ -352,7 +348,7 @@ def run_ours(args, rank, world, local):
                          "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": "sph_autotune"},
         # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, else 3), fill,
         # placement; plus the Shepard kernel on re-initialisation steps
-        "gpu_launches": args.steps * (4 + (1 if grid_cells(scene) <= 16384 else 3)) + reinit_steps,
+        "gpu_launches": args.steps * (4 + (1 if grid_cells(scene, prec) <= 16384 else 3)) + reinit_steps,
         "clocks": clocks,
     }
     return out
@@ -382,12 +378,14 @@ def run_batched(args):
     sc = scenes.batched_dam_breaks(512, seed=0)
     nf = sum(s.n_fluid for s in sc)
     nw = sum(s.n_wall for s in sc)
-    nc = sum(batch.footprint(s)[1] for s in sc)
+    nc = sum(batch.footprint(s, 1)[1] for s in sc)          # FP32 form (cells of r_cut)
+    nc64 = sum(batch.footprint(s, 0)[1] for s in sc)        # FP64 form (cells of r_cut / 2)
     res = {"workload": f"512 batched 2D dam breaks, {nf} fluid + {nw} wall particles, {nc} cells, CubicSpline, "
                        "FluidWallSolve, per-scene c0 and dt", "fluid_particles": nf,
            "l2": "state larger than L2 (no flush)"}
     for prec, steps in ((1, args.batched_steps), (0, 2)):
-        with batch.Batch(sc[0].params(precision=prec), nf + 1024, nc + 1024, nw + 1024, 512) as bt:
+        cells = (nc if prec == 1 else nc64) + 1024
+        with batch.Batch(sc[0].params(precision=prec), nf + 1024, cells, nw + 1024, 512) as bt:
             for s in sc:
                 bt.add_scene(s, 1, 1000)
             shape = bt.autotune(2) if prec == 1 else None
@@ -404,13 +402,16 @@ def run_batched(args):
 def run_served(args):
     """A Poisson stream of mixed scene requests (2D dam breaks, periodic 2D Poiseuille,
     3D dam breaks) served by continuous batching; latency p50/p99 and particle-steps/s,
-    FP32-compensated vs plain FP64 on the same stream (shorter step budgets for FP64)."""
+    FP32-compensated vs plain FP64 on the same (shorter) stream, plus a longer stream with
+    the full step budgets U{500..5000} in the FP32-compensated form."""
     import ethersph_gb300  # noqa: F401
     from ethersph_gb300 import scenes, serve
     out = {}
-    for prec, count, steps in ((1, args.served_requests, (500, 5000)), (0, max(6, args.served_requests // 8),
-                                                                          (100, 400))):
-        reqs = scenes.poisson_stream(rate=args.served_rate, count=count, seed=0, steps=steps)
+    runs = (("fp32c_full", 1, args.served_requests, (500, 5000), 1),
+            ("fp32c_short", 1, max(8, args.served_requests // 4), (200, 800), 2),
+            ("fp64_short", 0, max(8, args.served_requests // 4), (200, 800), 2))
+    for name, prec, count, steps, seed in runs:
+        reqs = scenes.poisson_stream(rate=args.served_rate, count=count, seed=seed, steps=steps)
         srv = serve.Server(budget_bytes=150e9 if prec == 1 else 40e9, precision=prec)
         try:
             rep = srv.run(reqs)
@@ -419,7 +420,10 @@ def run_served(args):
         s = rep.summary()
         s["rate_per_s"] = args.served_rate
         s["steps_per_request"] = list(steps)
-        out["fp32c" if prec == 1 else "fp64"] = s
+        s["stream_seed"] = seed
+        out[name] = s
+    out["fp32c_over_fp64_same_stream"] = (out["fp32c_short"]["particle_steps_per_s"] /
+                                          out["fp64_short"]["particle_steps_per_s"])
     out["workload"] = ("Poisson arrivals, 1/3 each 2D dam break (batched distribution), periodic 2D Poiseuille "
                        "(H=1mm, Re~U[0.01,1], dx=H/U{20..80}), 3D dam break (dx~U[0.01,0.02]); "
                        "150 GB device budget (FP64: 40 GB)")

@@ -47,7 +47,7 @@ class SphParams(C.Structure):
         ("check_enabled", C.c_int32), ("periodic_x", C.c_int32),
         ("check_lo", C.c_double * 3), ("check_hi", C.c_double * 3),
         ("domain_lo", C.c_double * 3), ("domain_hi", C.c_double * 3),
-        ("nan_check", C.c_int32), ("reserved0", C.c_int32),
+        ("nan_check", C.c_int32), ("cell_subdivision", C.c_int32),
     ]
 
 

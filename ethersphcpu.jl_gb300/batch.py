@@ -39,9 +39,17 @@ def merged_walls(scene):
     return dict(x=cat(xs), normal=cat(ns), gap=cat(gs), t=cat(ts), kappa=cat(ks), v=cat(vs), kind=cat(kinds))
 
 
-def grid_cells(scene) -> int:
-    """Cells of the scene's grid as the library builds it (edge r_cut (1 + 1e-9))."""
-    edge = scene.kernel.influence_radius_ * (1.0 + 1e-9)
+def cells_per_cutoff(cell_subdivision: int, precision: int, dim: int) -> int:
+    """The library's cell subdivision (its default: 1 for the FP32 form in 2D, else 2)."""
+    if cell_subdivision:
+        return cell_subdivision
+    return 1 if precision == _abi.PRECISION_FP32_COMPENSATED and dim == 2 else 2
+
+
+def grid_cells(scene, cell_subdivision: int = 0, precision: int = _abi.PRECISION_FP64) -> int:
+    """Cells of the scene's grid as the library builds it (edge r_cut (1 + 1e-9) / m)."""
+    m = cells_per_cutoff(cell_subdivision, precision, scene.kernel.dim_)
+    edge = scene.kernel.influence_radius_ * (1.0 + 1e-9) / m
     n = 1
     for a in range(scene.kernel.dim_):
         L = scene.domain_hi[a] - scene.domain_lo[a]
@@ -52,9 +60,9 @@ def grid_cells(scene) -> int:
     return n
 
 
-def footprint(scene) -> tuple[int, int, int]:
+def footprint(scene, precision: int = _abi.PRECISION_FP64) -> tuple[int, int, int]:
     """(particles, cells incl. the scene's sentinel cell, walls) the scene occupies."""
-    return scene.n_fluid, grid_cells(scene) + 1, scene.n_wall
+    return scene.n_fluid, grid_cells(scene, 0, precision) + 1, scene.n_wall
 
 
 def bytes_per(dim: int, thermal: bool, precision: int) -> tuple[int, int, int]:
@@ -163,7 +171,7 @@ class Batch:
         return dict(particles=out[0], cells=out[1], walls=out[2], scenes=out[3])
 
     def fits(self, scene) -> bool:
-        p, c, w = footprint(scene)
+        p, c, w = footprint(scene, self.precision)
         fr = self.free()
         return p <= fr["particles"] and c <= fr["cells"] and w <= fr["walls"] and fr["scenes"] >= 1
 

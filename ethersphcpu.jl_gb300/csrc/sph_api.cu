@@ -85,7 +85,15 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
         err = "influence_radius, h, dt and rho_0 must be positive"; return false;
     }
     const double rc = p.influence_radius;
-    const double edge = rc * (1.0 + 1e-9);
+    // cells per r_cut; default: 2 (fewer candidate pairs) except for the FP32 form in 2D,
+    // where the cheap candidate test makes the longer cell walk the larger cost
+    const int m = p.cell_subdivision != 0 ? p.cell_subdivision
+                                          : (p.precision == SPH_PRECISION_FP32_COMPENSATED && p.dim == 2 ? 1 : 2);
+    if (m != 1 && m != 2) { err = "cell_subdivision must be 0, 1 or 2"; return false; }
+    S.reach = m;
+    // cell edge r_cut (1 + 1e-9) / m: a pair with d <= r_cut is at most m cells apart
+    // even after rounding
+    const double edge = rc * (1.0 + 1e-9) / (double)m;
     int64_t ncells = 1;
     for (int a = 0; a < 3; ++a) {
         if (a >= p.dim) { S.n[a] = 1; S.lo[a] = 0.0; S.inv_cell[a] = 0.0; continue; }
@@ -95,7 +103,7 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
         if (a == 0 && p.periodic_x) {
             const double L = p.domain_hi[0] - p.domain_lo[0];
             na = (int64_t)std::floor(L / edge);
-            if (na < 3) { err = "a periodic axis needs at least 3 cells of edge r_cut"; return false; }
+            if (na < 2 * m + 1) { err = "a periodic axis needs at least 2 m + 1 cells"; return false; }
             S.cell_d[a] = L / (double)na;
             S.inv_cell[a] = 1.0 / S.cell_d[a];
         } else {

@@ -33,6 +33,8 @@ struct SceneDev {
     double inv_cell[3];
     double cell_d[3];   // cell edge per axis; cell c starts at lo + c * cell_d
     int32_t n[3];
+    int32_t reach;      // neighbour cells within +-reach (cells per r_cut)
+    int32_t pad_reach;
     int32_t cell_off;   // first global cell of this scene
     int32_t ncells;
     int32_t periodic_x;

@@ -109,36 +109,37 @@ __device__ __forceinline__ float kernel_w_f(float q, const SceneDev& S) {
     return W;
 }
 
-// Neighbour rows in (z, y) order; inside a row the cells x-1, x, x+1 (wrapping on a
-// periodic axis, skipped off the grid) form one virtual range that the TPP lanes share.
-// The callback gets the sorted index j and the offset of j's cell from i's cell (m).
+// Neighbour rows in (z, y) order (within +-reach cells); inside a row the cells
+// x-reach .. x+reach (wrapping on a periodic axis, skipped off the grid) form one virtual
+// range that the TPP lanes share.  The callback gets the sorted index j and the offset
+// of j's cell from i's cell in metres.
 template <int DIM, int TPP, typename F>
 __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
                                            int lane, F&& f) {
-    const int zr = DIM == 3 ? 1 : 0;
+    const int m = S.reach;
+    const int zr = DIM == 3 ? m : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
         const int z = c[2] + dz;
         if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -m; dy <= m; ++dy) {
             const int y = c[1] + dy;
             if (y < 0 || y >= S.n[1]) continue;
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
             const float oy = (float)dy * S.cell_f[1];
             const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
-            // the row's cells are one virtual range v = 0 .. len0+len1+len2-1; lane t
+            // the row's cells are one virtual range v = 0 .. (sum of lengths)-1; lane t
             // takes v = t, t+TPP, ...  Each cell is walked in turn from the first v of
-            // the lane inside it (unrolled: every index stays in a register).
+            // the lane inside it (scalars only: every index stays in a register).
             int prefix = 0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                int x = c[0] + k - 1;
+            for (int dx = -m; dx <= m; ++dx) {
+                int x = c[0] + dx;
                 bool ok = true;
                 if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 else ok = x >= 0 && x < S.n[0];
                 if (!ok) continue;
                 const int b = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
-                const float ox = (float)(k - 1) * S.cell_f[0];
+                const float ox = (float)dx * S.cell_f[0];
                 const int first = (lane - prefix) & (TPP - 1);
                 for (int j = b + first; j < e; j += TPP) f(j, ox, oy, oz);
                 prefix += e - b;

@@ -162,26 +162,28 @@ __device__ __forceinline__ double dotd(const double a[DIM], const double b[DIM])
 }
 
 // ---------------------------------------------------------------- neighbour walk
-// Visits the neighbour cells of cell c in (z, y, x) order, each x-run of up to three
-// cells as one contiguous range of the sorted arrays (cells of a row are adjacent in
-// key space).  A periodic x axis visits its three cells one by one (wrapping).
+// Visits the neighbour cells of cell c (within +-reach cells on every axis) in (z, y, x)
+// order, each x-run of up to 2 reach + 1 cells as one contiguous range of the sorted
+// arrays (cells of a row are adjacent in key space).  A periodic x axis visits its cells
+// one by one (wrapping; it has at least 2 reach + 1 cells, so none repeats).
 template <int DIM, typename F>
 __device__ __forceinline__ void walk_cells(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
                                            F&& f) {
-    const int zr = DIM == 3 ? 1 : 0;
+    const int m = S.reach;
+    const int zr = DIM == 3 ? m : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
         const int z = c[2] + dz;
         if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -m; dy <= m; ++dy) {
             const int y = c[1] + dy;
             if (y < 0 || y >= S.n[1]) continue;
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
             if (!S.periodic_x) {
-                const int x0 = c[0] > 0 ? c[0] - 1 : 0;
-                const int x1 = c[0] + 1 < S.n[0] ? c[0] + 1 : S.n[0] - 1;
+                const int x0 = c[0] > m ? c[0] - m : 0;
+                const int x1 = c[0] + m < S.n[0] ? c[0] + m : S.n[0] - 1;
                 f(__ldg(start + row + x0), __ldg(start + row + x1 + 1));
             } else {
-                for (int dx = -1; dx <= 1; ++dx) {
+                for (int dx = -m; dx <= m; ++dx) {
                     int x = c[0] + dx;
                     x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                     f(__ldg(start + row + x), __ldg(start + row + x + 1));

@@ -61,7 +61,7 @@ struct SphParams
     domain_lo::NTuple{3, Float64}
     domain_hi::NTuple{3, Float64}
     nan_check::Int32
-    reserved0::Int32
+    cell_subdivision::Int32
 end
 
 kernelCode(::CubicSpline) = Int32(0)

@@ -40,10 +40,11 @@ class Scene:
     periodic_x: bool = False
     meta: dict = field(default_factory=dict)
 
-    def params(self, precision: int = _abi.PRECISION_FP64, nan_check: bool = True) -> _abi.SphParams:
+    def params(self, precision: int = _abi.PRECISION_FP64, nan_check: bool = True,
+               cell_subdivision: int = 0) -> _abi.SphParams:
         return make_params(self.kernel, self.model, self.td, solve=self.solve, precision=precision,
                            check=self.check, domain_lo=self.domain_lo, domain_hi=self.domain_hi,
-                           periodic_x=self.periodic_x, nan_check=nan_check)
+                           periodic_x=self.periodic_x, nan_check=nan_check, cell_subdivision=cell_subdivision)
 
     @property
     def n_fluid(self) -> int:

@@ -97,7 +97,7 @@ class Server:
                 b = self.batches[dim]
                 while q:
                     r, scene = q[0]
-                    p, c, w = footprint(scene)
+                    p, c, w = footprint(scene, b.precision)
                     fr = b.free()
                     if not (p <= fr["particles"] and c <= fr["cells"] and w <= fr["walls"] and fr["scenes"] >= 1):
                         break

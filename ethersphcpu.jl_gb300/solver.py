@@ -27,7 +27,8 @@ from .types import (AABBCheck, CompulsiveWallParticles, StaticVelocityWallPartic
 
 
 def make_params(kernel, model, td, *, solve: int, precision: int = _abi.PRECISION_FP64, check: AABBCheck | None = None,
-                domain_lo=None, domain_hi=None, periodic_x: bool = False, nan_check: bool = True) -> _abi.SphParams:
+                domain_lo=None, domain_hi=None, periodic_x: bool = False, nan_check: bool = True,
+                cell_subdivision: int = 0) -> _abi.SphParams:
     """Fill the C parameter block from the Julia-mirror objects."""
     p = _abi.SphParams()
     p.dim = kernel.dim_
@@ -68,6 +69,7 @@ def make_params(kernel, model, td, *, solve: int, precision: int = _abi.PRECISIO
         p.domain_hi[k] = domain_hi[k] if domain_hi is not None and k < len(domain_hi) else 1.0
     p.periodic_x = 1 if periodic_x else 0
     p.nan_check = 1 if nan_check else 0
+    p.cell_subdivision = cell_subdivision
     return p
 
 

@@ -217,6 +217,7 @@ struct Model {
     double rho0, c0, p0, b, nu0, g[3], t0, kappa0, cp, beta, dt;
     int64_t reinit_interval, check_interval;
     int check_enabled, periodic_x;
+    int cells_per_rc;  // grid cells per r_cut along each axis
     double lo[3], hi[3];
     double dlo[3], dhi[3];
 };
@@ -240,6 +241,7 @@ struct Walls {
 // cells, which keeps adjacency (clamping is monotone and 1-Lipschitz on cells).
 struct Grid {
     int dim;
+    int m;  // neighbour cells within +-m
     double lo[3], inv[3];
     int64_t n[3];
     int periodic_x;
@@ -264,13 +266,14 @@ Grid make_grid(const Model& M, double rc) {
     G.dim = M.dim;
     G.periodic_x = M.periodic_x;
     G.period = M.dhi[0] - M.dlo[0];
-    const double edge = rc * (1.0 + 1e-9);
+    G.m = M.cells_per_rc;
+    const double edge = rc * (1.0 + 1e-9) / (double)G.m;
     for (int a = 0; a < 3; ++a) {
         G.lo[a] = M.dlo[a];
         if (a >= M.dim) { G.n[a] = 1; G.inv[a] = 0.0; continue; }
         if (a == 0 && M.periodic_x) {
             int64_t nx = (int64_t)std::floor(G.period / edge);
-            if (nx < 3) nx = 0;  // rejected by load_model: a periodic axis needs >= 3 cells
+            if (nx < 2 * G.m + 1) nx = 0;  // rejected by load_model: too few periodic cells
             G.n[a] = nx;
             G.inv[a] = 1.0 / (G.period / (double)nx);
         } else {
@@ -300,20 +303,22 @@ double dist2(const double* rv, int dim) {
 }
 
 // Neighbour cells of cell (cx, cy, cz) in visiting order: z, then y, then x, each
-// -1, 0, +1; cells off the grid are skipped, a periodic x axis wraps.
-int neighbour_cells(const Grid& G, const int64_t c[3], int64_t out[27]) {
+// -m .. +m; cells off the grid are skipped, a periodic x axis wraps.
+constexpr int kMaxCells = 125;  // (2 m + 1)^3 for m = 2
+int neighbour_cells(const Grid& G, const int64_t c[3], int64_t out[kMaxCells]) {
     int cnt = 0;
-    const int zr = G.dim == 3 ? 1 : 0;
+    const int m = G.m;
+    const int zr = G.dim == 3 ? m : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
         const int64_t z = c[2] + dz;
         if (z < 0 || z >= G.n[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -m; dy <= m; ++dy) {
             const int64_t y = c[1] + dy;
             if (y < 0 || y >= G.n[1]) continue;
-            for (int dx = -1; dx <= 1; ++dx) {
+            for (int dx = -m; dx <= m; ++dx) {
                 int64_t x = c[0] + dx;
                 if (G.periodic_x) {
-                    x = (x + G.n[0]) % G.n[0];  // n[0] >= 3, so the three cells are distinct
+                    x = (x + G.n[0]) % G.n[0];  // n[0] >= 2m+1, so no cell repeats
                 } else if (x < 0 || x >= G.n[0]) {
                     continue;
                 }
@@ -541,7 +546,7 @@ void build_lists(const Grid& G, const Kern& K, const Fluid& F, const Walls& W, c
         const double* xi = &F.x[i * dim];
         int64_t c[3];
         cell_of(G, xi, c);
-        int64_t cells[27];
+        int64_t cells[kMaxCells];
         const int nc = neighbour_cells(G, c, cells);
         for (int q = 0; q < nc; ++q) {
             for (int64_t s = CL.start[cells[q]]; s < CL.start[cells[q] + 1]; ++s) {
@@ -703,7 +708,7 @@ void step_gather(const Grid& G, const Kern& K, const Model& M, Fluid& F, const W
         const double* xi = &x0[i * dim];
         int64_t c[3];
         cell_of(G, xi, c);
-        int64_t cells[27];
+        int64_t cells[kMaxCells];
         const int nc = neighbour_cells(G, c, cells);
         double drho = 0.0;
         for (int q = 0; q < nc; ++q)
@@ -726,7 +731,7 @@ void step_gather(const Grid& G, const Kern& K, const Model& M, Fluid& F, const W
         const double* xi = &x0[i * dim];
         int64_t c[3];
         cell_of(G, xi, c);
-        int64_t cells[27];
+        int64_t cells[kMaxCells];
         const int nc = neighbour_cells(G, c, cells);
         double dv[3] = {0, 0, 0}, dT = 0.0;
         for (int q = 0; q < nc; ++q)
@@ -766,7 +771,7 @@ void step_gather(const Grid& G, const Kern& K, const Model& M, Fluid& F, const W
             const double* xi = &x0[i * dim];
             int64_t c[3];
             cell_of(G, xi, c);
-            int64_t cells[27];
+            int64_t cells[kMaxCells];
             const int nc = neighbour_cells(G, c, cells);
             double sw = 0.0, sws = 0.0;
             for (int q = 0; q < nc; ++q)
@@ -811,9 +816,13 @@ bool load_model(const SphParams* p, Model* M, Kern* K) {
     M->check_interval = p->check_interval;
     M->check_enabled = p->check_enabled;
     M->periodic_x = p->periodic_x;
+    // the library's default: 1 for the FP32 form in 2D, else 2
+    M->cells_per_rc = p->cell_subdivision != 0 ? p->cell_subdivision
+                                               : (p->precision == SPH_PRECISION_FP32_COMPENSATED && p->dim == 2 ? 1 : 2);
+    if (M->cells_per_rc != 1 && M->cells_per_rc != 2) return false;
     if (M->periodic_x) {
-        const double edge = K->rc * (1.0 + 1e-9);
-        if (!(std::floor((M->dhi[0] - M->dlo[0]) / edge) >= 3.0)) return false;
+        const double edge = K->rc * (1.0 + 1e-9) / (double)M->cells_per_rc;
+        if (!(std::floor((M->dhi[0] - M->dlo[0]) / edge) >= 2.0 * M->cells_per_rc + 1.0)) return false;
     }
     return true;
 }
@@ -903,7 +912,7 @@ int or_neighbour_counts(const SphParams* prm, int64_t n, const double* x, int64_
     for (int64_t i = 0; i < n; ++i) {
         int64_t c[3];
         cell_of(G, x + i * dim, c);
-        int64_t cells[27];
+        int64_t cells[kMaxCells];
         const int nc = neighbour_cells(G, c, cells);
         for (int q = 0; q < nc; ++q) {
             for (int64_t s = CL.start[cells[q]]; s < CL.start[cells[q] + 1]; ++s) {

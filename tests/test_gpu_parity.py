@@ -19,8 +19,8 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
-def run_gpu(pkg, scene, first, nsteps, precision=0):
-    prm = scene.params(precision=precision)
+def run_gpu(pkg, scene, first, nsteps, precision=0, sub=0):
+    prm = scene.params(precision=precision, cell_subdivision=sub)
     with pkg.Simulation(prm, scene.n_fluid, scene.n_wall) as sim:
         for w in scene.walls:
             sim.upload_walls(w)
@@ -30,9 +30,10 @@ def run_gpu(pkg, scene, first, nsteps, precision=0):
         return sim.download()
 
 
-def run_oracle(orc, scene, first, nsteps, threads=8):
+def run_oracle(orc, scene, first, nsteps, threads=8, sub=0):
     fluid, walls = orc.scene_arrays(scene)
-    return orc.run(scene.params(), fluid, walls, first, nsteps, mode=orc.GATHER, threads=threads)
+    return orc.run(scene.params(cell_subdivision=sub), fluid, walls, first, nsteps, mode=orc.GATHER,
+                   threads=threads)
 
 
 def compare(got, ref, tol, keys=("x", "v", "rho", "p", "c")):
@@ -62,10 +63,20 @@ def test_dam_break_one_step(pkg, orc):
     compare(run_gpu(pkg, s, 1, 1), run_oracle(orc, s, 1, 1), TOL_1)
 
 
-def test_dam_break_100_steps(pkg, orc):
+@pytest.mark.parametrize("sub", [1, 2])
+def test_dam_break_100_steps(pkg, orc, sub):
     s = scenes_mod().dam_break_2d(dx=0.02)
-    errs = compare(run_gpu(pkg, s, 1, 100), run_oracle(orc, s, 1, 100), TOL_100)
-    print("dam break 100 steps:", errs)
+    errs = compare(run_gpu(pkg, s, 1, 100, sub=sub), run_oracle(orc, s, 1, 100, sub=sub), TOL_100)
+    print(f"dam break 100 steps (cell subdivision {sub}):", errs)
+
+
+def test_3d_subdivisions_agree(pkg, orc):
+    # the cell size changes only the neighbour order: the two grids agree to rounding
+    s = scenes_mod().dam_break_3d(dx=0.04, tank=(0.8, 0.4, 0.4), column=(0.24, 0.2, 0.4))
+    a = run_gpu(pkg, s, 1, 20, sub=1)
+    b = run_gpu(pkg, s, 1, 20, sub=2)
+    compare(a, b, 1e-11)
+    compare(b, run_oracle(orc, s, 1, 20, sub=2), 1e-11)
 
 
 def test_thermal_cavity_100_steps(pkg, orc):

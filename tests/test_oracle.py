@@ -295,3 +295,18 @@ def test_hydrostatic_column_stays_near_rest(pkg, orc):
     out = orc.run(s.params(), fluid, walls, 1, 60, mode=orc.GATHER, threads=2)
     disp = np.abs(out["x"] - fluid["x"]).max()
     assert disp < 0.2 * 0.05
+
+
+def test_cell_subdivisions_enumerate_the_same_pairs(pkg, orc):
+    from ethersph_gb300 import scenes
+    for s in (scenes.dam_break_2d(dx=0.05), scenes.dam_break_3d(dx=0.05, tank=(0.8, 0.4, 0.4),
+                                                                 column=(0.3, 0.2, 0.4))):
+        wx = s.walls[0].x_vec_
+        a = orc.neighbour_counts(s.params(cell_subdivision=1), s.fluid.x_vec_, wx)
+        b = orc.neighbour_counts(s.params(cell_subdivision=2), s.fluid.x_vec_, wx)
+        assert a == b
+        fluid, walls = orc.scene_arrays(s)
+        ra = orc.run(s.params(cell_subdivision=1), fluid, walls, 1, 6, mode=orc.GATHER, threads=2)
+        rb = orc.run(s.params(cell_subdivision=2), fluid, walls, 1, 6, mode=orc.GATHER, threads=2)
+        for k in ("x", "v", "rho"):
+            assert _rel(ra[k], rb[k]) < 1e-12, k
