@@ -6,6 +6,7 @@ import shutil
 import subprocess
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -78,3 +79,21 @@ def test_params_from_scene(pkg):
     assert p.h == s.kernel.h_ and p.sigma == s.kernel.sigma_
     assert p.density_reinitialized_interval == 30
     assert p.check_enabled == 0
+
+
+def test_vtp_writer_roundtrip(tmp_path, pkg):
+    from ethersph_gb300 import scenes, vtp
+    s = scenes.natural_convection_2d(n=16)
+    io = vtp.VTPIO(4, "cavity_", ".vtp", str(tmp_path), [":rho_", ":p_", ":c_", ":t_"],
+                   ["Density", "Pressure", "SoundSpeed", "Temperature"])
+    path = io.write(3, 0.25, s.fluid, s.walls)
+    assert path.endswith("cavity_0003.vtp")
+    a = vtp.read_vtp_arrays(path)
+    n = s.n_fluid + s.n_wall
+    assert a["Points"].shape == (n, 3)
+    assert np.array_equal(a["Points"][: s.n_fluid, :2], s.fluid.x_vec_)
+    assert np.all(a["Type"][: s.n_fluid] == 1) and set(a["Type"][s.n_fluid:]) == {2, 3}
+    assert np.array_equal(a["Temperature"][: s.n_fluid], s.fluid.t_)
+    # walls have no density field and no velocity: NaN, as writeVTP writes them
+    assert np.all(np.isnan(a["Density"][s.n_fluid:])) and np.all(np.isnan(a["Velocity"][s.n_fluid:]))
+    assert a["Step"][0] == 3 and a["Time"][0] == 0.25
