@@ -177,7 +177,8 @@ def test_stats_mass_exact(pkg):
         m0 = sim.stats().total_mass
         sim.step(1, 50)
         st = sim.stats()
-    assert st.total_mass == m0
+    # masses never change; the FP64 sum follows the cell-sorted order (last-bit effects)
+    assert st.total_mass == pytest.approx(m0, rel=1e-14)
     assert st.n_fluid == s.n_fluid
     assert st.steps_done == 50
 

@@ -81,6 +81,10 @@ def test_3d_dam_break_conserves_mass(pkg):
         m0 = sim.stats().total_mass
         sim.step(1, 400)
         st = sim.stats()
+        masses = sim.download()["mass"]
     assert st.n_fluid == s.n_fluid
-    assert st.total_mass == m0
+    # every particle keeps its mass exactly; the FP64 sum is taken in the current
+    # (cell-sorted) order, so it may differ from the initial sum in the last bit
+    assert np.array_equal(np.sort(masses), np.sort(s.fluid.mass_))
+    assert st.total_mass == pytest.approx(m0, rel=1e-14)
     assert st.kinetic_energy > 0.0 and np.isfinite(st.max_speed)
