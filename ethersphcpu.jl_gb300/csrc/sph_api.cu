@@ -1236,7 +1236,7 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         // overwrite them, so park them in the idle sorted buffer meanwhile
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].p, h->S[par].p, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].c, h->S[par].c, nbytes, cudaMemcpyDeviceToDevice, st));
-        const int tpps[4] = {1, 2, 4, 8};
+        const int tpps[5] = {-1, 1, 2, 4, 8};  // -1: one lane, software-pipelined loop
         const int blocks[3] = {64, 128, 256};
         int best_tpp[3] = {4, 4, 4};
         int best_block[3] = {128, 128, 128};
@@ -1287,8 +1287,8 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
     if (!h || !shape) return fail(h, SPH_ERR_ARG, "null argument");
     for (int k = 0; k < 3; ++k)
-        if (shape[k] != 1 && shape[k] != 2 && shape[k] != 4 && shape[k] != 8)
-            return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4 or 8");
+        if (shape[k] != -1 && shape[k] != 1 && shape[k] != 2 && shape[k] != 4 && shape[k] != 8)
+            return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
     if (shape[3] < 32 || shape[3] > 1024 || shape[3] % 32 != 0)
         return fail(h, SPH_ERR_ARG, "block size must be a multiple of 32 in [32, 1024]");
     for (int k = 0; k < 4; ++k) h->tune[k] = shape[k];

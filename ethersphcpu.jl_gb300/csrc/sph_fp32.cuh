@@ -1,4 +1,4 @@
-// sph_fp32.cu — FP32-compensated form of the continuity, momentum and Shepard gathers.
+// sph_fp32.cuh — FP32-compensated form of the continuity, momentum and Shepard gathers
 //
 // Pair arithmetic runs in FP32 on cell-relative positions: every particle carries
 // (x - origin of its cell) as floats, and a neighbour in the cell offset (dx, dy, dz)
@@ -20,6 +20,8 @@
 // Same terms, order of walls after fluid, and solve variants as sph_fp64.cu; the
 // formulas follow Continuity.jl, PressureForce.jl, ViscosityForce.jl, WallForce.jl,
 // ThermalConduction.jl, SelfAction/*.jl and ReconstructValue.jl.
+#pragma once
+
 #include "sph_physics.cuh"
 #include "sph_kernels.h"
 
@@ -148,6 +150,81 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
     }
 }
 
+// The same walk, software-pipelined: the loads of a lane's next candidate (load(j)) are
+// issued before the current candidate is processed (f(j, data, ...)), so the memory
+// latency of one overlaps the arithmetic of the other.  Few warps per scheduler (small
+// scenes) cannot hide that latency by switching warps.
+template <int DIM, int TPP, typename L, typename F>
+__device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* __restrict__ start,
+                                              const int32_t c[3], int lane, L&& load, F&& f) {
+    const int m = S.reach;
+    const int zr = DIM == 3 ? m : 0;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const int z = c[2] + dz;
+        if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
+        for (int dy = -m; dy <= m; ++dy) {
+            const int y = c[1] + dy;
+            if (y < 0 || y >= S.n[1]) continue;
+            const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
+            const float oy = (float)dy * S.cell_f[1];
+            const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
+            int prefix = 0;
+            for (int dx = -m; dx <= m; ++dx) {
+                int x = c[0] + dx;
+                bool ok = true;
+                if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
+                else ok = x >= 0 && x < S.n[0];
+                if (!ok) continue;
+                const int b = __ldg(start + row + x);
+                const int e = __ldg(start + row + x + 1);
+                const float ox = (float)dx * S.cell_f[0];
+                int j = b + ((lane - prefix) & (TPP - 1));
+                prefix += e - b;
+                if (j >= e) continue;
+                auto d = load(j);
+                for (;;) {
+                    const int jn = j + TPP;
+                    const bool more = jn < e;
+                    decltype(d) dn = d;
+                    if (more) dn = load(jn);
+                    f(j, d, ox, oy, oz);
+                    if (!more) break;
+                    j = jn;
+                    d = dn;
+                }
+            }
+        }
+    }
+}
+
+// Walk with (PF) or without software pipelining; body(j, load(j), ox, oy, oz).
+template <int DIM, int TPP, bool PF, typename L, typename F>
+__device__ __forceinline__ void walk(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
+                                     int lane, L&& load, F&& body) {
+    if constexpr (PF) {
+        walk_lanes_pf<DIM, TPP>(S, start, c, lane, load, body);
+    } else {
+        walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz) {
+            body(j, load(j), ox, oy, oz);
+        });
+    }
+}
+
+struct Cand2 {
+    float4 a, b;
+};
+struct Cand3 {
+    float4 a, b, c;
+};
+struct WallCand {
+    float4 a, b, c;
+    int kind;
+};
+struct CandShep {
+    float4 a;
+    double vol, m;
+};
+
 __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int32_t c[3]) {
     const int32_t k = key - S.cell_off;
     c[0] = k % S.n[0];
@@ -156,7 +233,7 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 }
 
 // -------------------------------------------------------------------- K4 (FP32)
-template <int DIM, int KK, int TPP>
+template <int DIM, int KK, int TPP, bool PF>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
@@ -178,10 +255,11 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
     int32_t c[3];
     decode_cell(st.cell[i], S, c);
     Kahan drho;
-    walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz) {
+    auto load = [&](int j) { return Cand2{st.fa[j], st.fb[j]}; };
+    walk<DIM, TPP, PF>(S, start, c, lane, load, [&](int j, const Cand2& cd, float ox, float oy, float oz) {
         if (j == i) return;
-        const float4 aj = st.fa[j];
-        const float4 bj = st.fb[j];  // loaded with aj: one round trip per candidate
+        const float4 aj = cd.a;
+        const float4 bj = cd.b;
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
         const float d2 = rx * rx + ry * ry + rz * rz;
@@ -230,7 +308,7 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
 }
 
 // -------------------------------------------------------------------- K5 (FP32)
-template <int DIM, int KK, int MODE, int TPP>
+template <int DIM, int KK, int MODE, int TPP, bool PF>
 __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
                                SortScratch sc, int32_t cap) {
     using V = typename VecT<DIM>::T;
@@ -273,14 +351,21 @@ __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState 
     decode_cell(st.cell[i], S, c);
     Kahan dv[3], dT;
 
-    walk_lanes<DIM, TPP>(S, sc.start, c, lane, [&](int j, float ox, float oy, float oz) {
+    // every load of a candidate is issued before its distance test (one memory round
+    // trip per candidate), and before the previous candidate is processed
+    auto load_f = [&](int j) {
+        Cand3 d;
+        d.a = st.fa[j];
+        d.b = st.fb[j];
+        d.c = (DIM == 3 || MODE == kModeThermal) ? st.fc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        return d;
+    };
+    walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, [&](int j, const Cand3& cd, float ox, float oy,
+                                                              float oz) {
         if (j == i) return;
-        // issue every load of the candidate before the distance test: one memory
-        // round trip per candidate instead of two for the accepted ones
-        const float4 aj = st.fa[j];
-        const float4 bj = st.fb[j];
-        float4 cj = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (DIM == 3 || MODE == kModeThermal) cj = st.fc[j];
+        const float4 aj = cd.a;
+        const float4 bj = cd.b;
+        const float4 cj = cd.c;
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
         const float d2 = rx * rx + ry * ry + rz * rz;
@@ -325,9 +410,19 @@ __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState 
     });
 
     if (wl.n > 0) {
-        walk_lanes<DIM, TPP>(S, wl.start, c, lane, [&](int w, float ox, float oy, float oz) {
-            const float4 wa = wl.fa[w];
-            const float4 wb = wl.fb[w];
+        auto load_w = [&](int w) {
+            WallCand d;
+            d.a = wl.fa[w];
+            d.b = wl.fb[w];
+            d.c = (DIM == 3 || MODE == kModeThermal) ? wl.fc[w] : make_float4(0.f, 0.f, 0.f, 0.f);
+            d.kind = (DIM == 3 && MODE == kModeThermal) ? wl.kind[w] : 0;
+            return d;
+        };
+        walk<DIM, TPP, PF>(S, wl.start, c, lane, load_w, [&](int w, const WallCand& cd, float ox, float oy,
+                                                                   float oz) {
+            const float4 wa = cd.a;
+            const float4 wb = cd.b;
+            const float4 wc = cd.c;
             float rv[3], n[3], vv[3], gw, Tw = 0.f, kw = 0.f;
             bool thermo = false;
             if (DIM == 2) {
@@ -336,17 +431,15 @@ __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState 
                 vv[0] = vi[0] - wb.x; vv[1] = vi[1] - wb.y; vv[2] = 0.f;
                 gw = wb.z;
                 if (MODE == kModeThermal) {
-                    const float4 wc = wl.fc[w];
                     Tw = wb.w; kw = wc.x; thermo = wc.y != 0.f;
                 }
             } else {
                 rv[0] = xi[0] - ox - wa.x; rv[1] = xi[1] - oy - wa.y; rv[2] = xi[2] - oz - wa.z;
                 gw = wa.w;
                 n[0] = wb.x; n[1] = wb.y; n[2] = wb.z;
-                const float4 wc = wl.fc[w];
                 vv[0] = vi[0] - wc.x; vv[1] = vi[1] - wc.y; vv[2] = vi[2] - wc.z;
                 if (MODE == kModeThermal) {
-                    Tw = wb.w; kw = wc.w; thermo = wl.kind[w] == SPH_WALL_THERMOSTATIC;
+                    Tw = wb.w; kw = wc.w; thermo = cd.kind == SPH_WALL_THERMOSTATIC;
                 }
             }
             const float d2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
@@ -471,7 +564,7 @@ __global__ void k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState 
 }
 
 // -------------------------------------------------------------------- K6 (FP32 W, FP64 sums)
-template <int DIM, int KK, int TPP>
+template <int DIM, int KK, int TPP, bool PF>
 __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, SortScratch sc,
                              int32_t cap, int force) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -486,16 +579,18 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
     int32_t c[3];
     decode_cell(st.cell[i], S, c);
     double sw = 0.0, sws = 0.0;
-    walk_lanes<DIM, TPP>(S, sc.start, c, lane, [&](int j, float ox, float oy, float oz) {
+    auto load = [&](int j) { return CandShep{st.fa[j], st.vol[j], st.m[j]}; };
+    walk<DIM, TPP, PF>(S, sc.start, c, lane, load, [&](int j, const CandShep& cd, float ox, float oy,
+                                                            float oz) {
         if (j == i) return;
-        const float4 aj = st.fa[j];
+        const float4 aj = cd.a;
         const float rx = xi0 - ox - aj.x, ry = xi1 - oy - aj.y;
         const float rz = DIM == 3 ? xi2 - oz - aj.z : 0.f;
         const float d2 = rx * rx + ry * ry + rz * rz;
         if (!(d2 <= S.rc2_f)) return;
         const double W = (double)kernel_w_f<KK>(sqrtf(d2) * S.inv_h_f, S);
-        sw += W * st.vol[j];
-        sws += W * st.m[j];
+        sw += W * cd.vol;
+        sws += W * cd.m;
     });
     const unsigned mask = group_mask<TPP>();
     sw = group_sum<TPP>(sw, mask);
@@ -507,34 +602,38 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
 }
 
 // -------------------------------------------------------------------- launchers
-template <int DIM, int KK, int TPP>
+template <int DIM, int KK, int TPP, bool PF>
 void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        k_continuity_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
+        k_continuity_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
     } else if (stage == 2) {
-        k_reinit_f32<DIM, KK, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap, L.force_reinit);
+        k_reinit_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap,
+                                                                      L.force_reinit);
     } else if (mode == kModeFluidWall) {
-        k_momentum_f32<DIM, KK, kModeFluidWall, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc,
-                                                                                   L.cap);
+        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
+                                                                                       L.sc, L.cap);
     } else if (mode == kModeWallPressure) {
-        k_momentum_f32<DIM, KK, kModeWallPressure, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
-                                                                                      L.sc, L.cap);
+        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx,
+                                                                                          L.wl, L.sc, L.cap);
     } else {
-        k_momentum_f32<DIM, KK, kModeThermal, TPP><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc,
-                                                                                 L.cap);
+        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
+                                                                                     L.sc, L.cap);
     }
 }
 
+// Lanes code: 1, 2, 4, 8 lanes per particle; -1: one lane with a software-pipelined
+// candidate loop (pays off when few warps are resident, i.e. small scenes).
 template <int DIM, int KK>
 void launch_kk(int stage, const LaunchCtx& L) {
     const int tpp = stage == 0 ? L.tpp_continuity : (stage == 1 ? L.tpp_momentum : L.tpp_reinit);
     switch (tpp) {
-        case 1: launch_tpp<DIM, KK, 1>(stage, L.mode, L); break;
-        case 2: launch_tpp<DIM, KK, 2>(stage, L.mode, L); break;
-        case 8: launch_tpp<DIM, KK, 8>(stage, L.mode, L); break;
-        default: launch_tpp<DIM, KK, 4>(stage, L.mode, L); break;
+        case -1: launch_tpp<DIM, KK, 1, true>(stage, L.mode, L); break;
+        case 1: launch_tpp<DIM, KK, 1, false>(stage, L.mode, L); break;
+        case 2: launch_tpp<DIM, KK, 2, false>(stage, L.mode, L); break;
+        case 8: launch_tpp<DIM, KK, 8, false>(stage, L.mode, L); break;
+        default: launch_tpp<DIM, KK, 4, false>(stage, L.mode, L); break;
     }
 }
 
@@ -549,10 +648,5 @@ void dispatch(int stage, const LaunchCtx& L) {
 }
 
 }  // namespace
-
-void launch_physics_fp32(int stage, const LaunchCtx& L) {
-    if (L.dim == 2) dispatch<2>(stage, L);
-    else dispatch<3>(stage, L);
-}
 
 }  // namespace sph

@@ -33,6 +33,8 @@ struct LaunchCtx {
 // stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init
 void launch_physics_fp64(int stage, const LaunchCtx& L);
 void launch_physics_fp32(int stage, const LaunchCtx& L);
+void launch_physics_fp32_2d(int stage, const LaunchCtx& L);
+void launch_physics_fp32_3d(int stage, const LaunchCtx& L);
 
 // Cell hash of the unsorted positions in L.nx.x (used once after an upload).
 void launch_hash(const LaunchCtx& L);

@@ -292,7 +292,7 @@ int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double
                                 const double* wall_x, int64_t* counts, void* stream);
 
 /* Autotuner of the FP32-compensated form: times the continuity, momentum and Shepard
- * gathers on the current state for every lanes-per-particle count {1, 2, 4, 8} and
+ * gathers on the current state for every lanes-per-particle count {-1, 1, 2, 4, 8} and
  * block size {64, 128, 256}, keeps the fastest for each stage and rebuilds the step
  * graphs.  out[4] (may be NULL) receives (continuity lanes, momentum lanes, Shepard
  * lanes, block size).  The fluid state is left unchanged.  No-op for the FP64 form,
@@ -300,9 +300,11 @@ int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 
 /* Set the FP32 launch shape by hand: shape[4] = (continuity lanes, momentum lanes,
- * Shepard lanes, block size); lanes in {1, 2, 4, 8}, block in {32, 64, ..., 1024} and a
- * multiple of 32.  Results of the FP32 form depend on the lane count (the order of the
- * compensated partial sums), never on the block size. */
+ * Shepard lanes, block size); lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
+ * is software-pipelined: loads of the next neighbour overlap the current one's
+ * arithmetic), block in {32, 64, ..., 1024} and a multiple of 32.  Results of the FP32
+ * form depend on the lane count (the order of the compensated partial sums; -1 sums like
+ * 1), never on the block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
 
 /* Text of the last error on this handle (or of the last failed sph_create when h is NULL). */

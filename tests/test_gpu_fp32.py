@@ -49,7 +49,7 @@ def test_fp32_form_within_1e4_after_1000_steps(pkg, name):
     assert np.array_equal(a["mass"], b["mass"])
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+@pytest.mark.parametrize("lanes", [-1, 1, 2, 4, 8])
 def test_every_lane_count(pkg, lanes):
     # each lanes-per-particle variant of the three FP32 gathers, against the FP64 form
     s = scenes_mod().natural_convection_2d(n=48)
