@@ -370,19 +370,23 @@ def time_batch_steps(bt, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def run_batched(args):
+def run_batched(args, rank=0, world=1):
     """512 seeded 2D dam breaks (dx 0.01, 450-67,500 fluid particles each) stepped in one
-    set of launches: FP32-compensated with an autotuned launch shape, and plain FP64."""
+    set of launches: FP32-compensated with an autotuned launch shape, and plain FP64.
+    Under torchrun every rank steps its share of the scenes (k % world == rank); the
+    slowest rank's time and all ranks' particles give the whole-job rate."""
     import ethersph_gb300  # noqa: F401
-    from ethersph_gb300 import batch, scenes
-    sc = scenes.batched_dam_breaks(512, seed=0)
+    from ethersph_gb300 import batch, distributed, scenes
+    every = scenes.batched_dam_breaks(512, seed=0)
+    sc = distributed.shard(every, rank, world)
     nf = sum(s.n_fluid for s in sc)
     nw = sum(s.n_wall for s in sc)
     nc = sum(batch.footprint(s, 1)[1] for s in sc)          # FP32 form (cells of r_cut)
     nc64 = sum(batch.footprint(s, 0)[1] for s in sc)        # FP64 form (cells of r_cut / 2)
-    res = {"workload": f"512 batched 2D dam breaks, {nf} fluid + {nw} wall particles, {nc} cells, CubicSpline, "
-                       "FluidWallSolve, per-scene c0 and dt", "fluid_particles": nf,
-           "l2": "state larger than L2 (no flush)"}
+    nf_all = sum(s.n_fluid for s in every)
+    res = {"workload": f"512 batched 2D dam breaks, {nf_all} fluid + {sum(s.n_wall for s in every)} wall "
+                       "particles, CubicSpline, FluidWallSolve, per-scene c0 and dt", "fluid_particles": nf_all,
+           "l2": "state larger than L2 (no flush)", "ranks": world}
     for prec, steps in ((1, args.batched_steps), (0, 2)):
         cells = (nc if prec == 1 else nc64) + 1024
         with batch.Batch(sc[0].params(precision=prec), nf + 1024, cells, nw + 1024, 512) as bt:
@@ -390,8 +394,9 @@ def run_batched(args):
                 bt.add_scene(s, 1, 1000)
             shape = bt.autotune(2) if prec == 1 else None
             ms = time_batch_steps(bt, steps, 2)
+            ms_all, _, rate = distributed.aggregate(ms, nf, device="cuda")
             key = "fp32c" if prec == 1 else "fp64"
-            res[key] = {"ms_per_step": ms, "particle_steps_per_s": nf / (ms / 1e3), "steps": steps}
+            res[key] = {"ms_per_step": ms_all, "particle_steps_per_s": rate, "steps": steps}
             if shape:
                 res[key]["launch_shape"] = shape
                 res[key]["stages_ms"] = bt.time_stages(3)
@@ -399,25 +404,26 @@ def run_batched(args):
     return res
 
 
-def run_served(args):
+def run_served(args, rank=0, world=1):
     """A Poisson stream of mixed scene requests (2D dam breaks, periodic 2D Poiseuille,
     3D dam breaks) served by continuous batching; latency p50/p99 and particle-steps/s,
     FP32-compensated vs plain FP64 on the same (shorter) stream, plus a longer stream with
     the full step budgets U{500..5000} in the FP32-compensated form."""
     import ethersph_gb300  # noqa: F401
-    from ethersph_gb300 import scenes, serve
+    from ethersph_gb300 import distributed, scenes, serve
     out = {}
     runs = (("fp32c_full", 1, args.served_requests, (500, 5000), 1),
             ("fp32c_short", 1, max(8, args.served_requests // 4), (200, 800), 2),
             ("fp64_short", 0, max(8, args.served_requests // 4), (200, 800), 2))
     for name, prec, count, steps, seed in runs:
-        reqs = scenes.poisson_stream(rate=args.served_rate, count=count, seed=seed, steps=steps)
+        reqs = distributed.shard(scenes.poisson_stream(rate=args.served_rate, count=count, seed=seed, steps=steps),
+                                 rank, world)
         srv = serve.Server(budget_bytes=150e9 if prec == 1 else 40e9, precision=prec)
         try:
             rep = srv.run(reqs)
         finally:
             srv.close()
-        s = rep.summary()
+        s = serve.summarize_ranks(rep, world)
         s["rate_per_s"] = args.served_rate
         s["steps_per_request"] = list(steps)
         s["stream_seed"] = seed
@@ -462,11 +468,13 @@ def main():
             dist.destroy_process_group()
         return
     out = run_ours(args, rank, world, local)
+    batched = run_batched(args, rank, world) if not (args.no_batched or args.only_steps) else None
+    served = run_served(args, rank, world) if not (args.no_served or args.only_steps) else None
     if rank == 0 and out is not None:
-        if not args.no_batched:
-            out["batched"] = run_batched(args)
-        if not args.no_served:
-            out["served"] = run_served(args)
+        if batched:
+            out["batched"] = batched
+        if served:
+            out["served"] = served
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(workload(args.n), args)
         print(json.dumps(out))

@@ -53,6 +53,31 @@ class Report:
         }
 
 
+def summarize_ranks(report: Report, world: int = 1) -> dict:
+    """Report.summary() over every rank of a sharded stream: the slowest rank's wall
+    time, all ranks' particle-steps, and percentiles over all ranks' latencies.  Every
+    rank must call it (it gathers); with one rank it is the local summary."""
+    if world <= 1:
+        return report.summary()
+    import torch.distributed as dist
+    mine = (report.wall_s, report.particle_steps, [c.latency for c in report.completed])
+    every = [None] * world
+    dist.all_gather_object(every, mine)
+    wall = max(w for w, _, _ in every)
+    steps = sum(p for _, p, _ in every)
+    lat = np.array([x for _, _, ls in every for x in ls]) if any(ls for _, _, ls in every) else np.zeros(1)
+    return {
+        "requests": sum(len(ls) for _, _, ls in every),
+        "wall_s": wall,
+        "particle_steps": steps,
+        "particle_steps_per_s": steps / wall if wall > 0 else 0.0,
+        "latency_p50_s": float(np.percentile(lat, 50)),
+        "latency_p99_s": float(np.percentile(lat, 99)),
+        "latency_mean_s": float(lat.mean()),
+        "ranks": world,
+    }
+
+
 class Server:
     def __init__(self, budget_bytes: float = 150e9, precision: int = _abi.PRECISION_FP32_COMPENSATED,
                  share_3d: float = 0.4, bundle: int = 10, scene_capacity: int = 4096, keep_results: bool = False,
