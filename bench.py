@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--batched-steps", type=int, default=20)
     ap.add_argument("--served-requests", type=int, default=48)
     ap.add_argument("--served-rate", type=float, default=100.0)
+    ap.add_argument("--launch-shape", default="",
+                    help="FP32 launch shape 'lanes,lanes,lanes,block' instead of the autotuner's pick")
     ap.add_argument("--only-steps", action="store_true",
                     help="upload, warm up and run the timed steps only (the command profiled with ncu)")
     return ap.parse_args()
@@ -231,7 +233,13 @@ def run_ours(args, rank, world, local):
     for w in scene.walls:
         sim.upload_walls(w)
     sim.upload_fluid(scene.fluid)
-    launch_shape = sim.autotune(3)  # lanes per particle x block size, picked on this scene
+    if args.launch_shape:
+        launch_shape = tuple(int(v) for v in args.launch_shape.split(","))
+        sim.set_launch_shape(*launch_shape)
+        chosen_by = "--launch-shape"
+    else:
+        launch_shape = sim.autotune(3)  # lanes per particle x block size, picked on this scene
+        chosen_by = "sph_autotune"
     lib, h = sim.lib, sim.h
     stream = torch.cuda.ExternalStream(sim.stream())
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -345,7 +353,7 @@ def run_ours(args, rank, world, local):
                 "what": f"upload + {e2e_steps} steps + download per iteration, {e2e_iters} iterations"},
         "plain_fp64": other,
         "launch_shape": {"continuity_lanes": launch_shape[0], "momentum_lanes": launch_shape[1],
-                         "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": "sph_autotune"},
+                         "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": chosen_by},
         # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, else 3), fill,
         # placement; plus the Shepard kernel on re-initialisation steps
         "gpu_launches": args.steps * (4 + (1 if grid_cells(scene, prec) <= 16384 else 3)) + reinit_steps,

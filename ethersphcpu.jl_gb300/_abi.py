@@ -19,6 +19,7 @@ SPH_OK = 0
 ERRORS = {
     1: "SPH_ERR_ARG", 2: "SPH_ERR_CUDA", 3: "SPH_ERR_OOM", 4: "SPH_ERR_NAN",
     5: "SPH_ERR_GRID_OVERFLOW", 6: "SPH_ERR_TIMEOUT", 7: "SPH_ERR_STATE", 8: "SPH_ERR_NO_DEVICE",
+    9: "SPH_ERR_IO",
 }
 KERNELS = {"CubicSpline": 0, "Gaussian": 1, "WendlandC2": 2, "WendlandC4": 3}
 SOLVE_FLUID_WALL = 0
@@ -77,6 +78,10 @@ SIGNATURES = {
     "sph_count_pairs": (C.c_int32, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_get_stream": (C.c_int32, [_H, C.POINTER(C.c_void_p)]),
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
+    "sph_output_open": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
+                                    C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_char_p]),
+    "sph_output_write": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),
+    "sph_output_flush": (C.c_int32, [C.c_void_p]),
     "sph_count_pairs_noalloc": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
                                             C.c_void_p, C.c_void_p]),
     "sph_batch_create": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_int64, C.c_int64, C.c_int32,

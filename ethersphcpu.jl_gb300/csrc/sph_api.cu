@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "sph_kernels.h"
+#include "sph_output.h"
 
 using namespace sph;
 
@@ -214,6 +215,7 @@ struct SceneRec {
     int64_t step_host = 1;  // mirror of the scene's device step counter
     std::vector<double> wx, wn, wv, wgap, wT, wkappa;  // host copy of the walls
     std::vector<int32_t> wkind;
+    std::vector<int64_t> wgroup_end;  // end of each sph_upload_walls group in the host copy
 };
 
 // First-fit allocator of ranges in [0, cap).
@@ -295,6 +297,8 @@ struct SphHandle {
     RangeAlloc cells, walls;
     // graph cache: key = (parity, pattern of Shepard steps) -> executable graph
     std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
+    sph::VtpWriter* out = nullptr;  // VTP output (sph_output_open)
+    int64_t out_walls = -1;         // wall groups the writer holds
 };
 
 namespace {
@@ -909,6 +913,7 @@ int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
     if ((int64_t)R.wgap.size() + n > R.wall_cap) return fail(h, SPH_ERR_GRID_OVERFLOW, "wall count exceeds the handle capacity");
     int32_t rc = add_walls_host(h, R, kind, n, x, normal, gap, t, kappa, v);
     if (rc != SPH_OK) return rc;
+    R.wgroup_end.push_back((int64_t)R.wgap.size());
     return write_scene_walls(h, 0);
 }
 
@@ -1299,8 +1304,85 @@ int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
 
 const char* sph_last_error(const SphHandle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
+int32_t sph_output_open(SphHandle* h, const char* dir_path, const char* file_name, const char* file_suffix,
+                        int32_t step_digit, int32_t n_fields, const char* const* field_symbols,
+                        const char* const* field_names, const char* wall_time) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "VTP output is for single-scene handles");
+    int dev = 0;
+    SPH_CUDA(h, cudaGetDevice(&dev));
+    if (!h->out) h->out = new sph::VtpWriter();
+    h->out_walls = -1;
+    std::string err;
+    int rc = h->out->open(dev, h->dim, h->thermal != 0, h->cap, dir_path, file_name, file_suffix, step_digit,
+                          n_fields, field_symbols, field_names, wall_time, err);
+    if (rc != SPH_OK) {
+        delete h->out;
+        h->out = nullptr;
+        return fail(h, rc, err);
+    }
+    return SPH_OK;
+}
+
+int32_t sph_output_write(SphHandle* h, int64_t file_step, double time) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->out || !h->out->is_open()) return fail(h, SPH_ERR_STATE, "sph_output_write before sph_output_open");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_output_write before sph_upload_fluid");
+    const SceneRec& R = h->scenes[0];
+    std::string err;
+    if (h->out_walls != (int64_t)R.wgroup_end.size()) {  // wall groups changed: hand the writer a copy
+        std::vector<sph::WallGroupHost> groups;
+        int64_t b = 0;
+        const int dim = h->dim;
+        for (int64_t e : R.wgroup_end) {
+            sph::WallGroupHost g;
+            g.kind = e > b ? R.wkind[b] : SPH_WALL_COMPULSIVE;
+            g.n = e - b;
+            g.x.assign(R.wx.begin() + b * dim, R.wx.begin() + e * dim);
+            g.v.assign(R.wv.begin() + b * dim, R.wv.begin() + e * dim);
+            g.gap.assign(R.wgap.begin() + b, R.wgap.begin() + e);
+            g.T.assign(R.wT.begin() + b, R.wT.begin() + e);
+            g.kappa.assign(R.wkappa.begin() + b, R.wkappa.begin() + e);
+            groups.push_back(std::move(g));
+            b = e;
+        }
+        int rc = h->out->set_walls(groups, err);
+        if (rc != SPH_OK) return fail(h, rc, err);
+        h->out_walls = (int64_t)R.wgroup_end.size();
+    }
+    const SortedState& d = h->S[h->par];
+    sph::FluidSnapshotSrc src{};
+    src.x = d.x;
+    src.v = d.v;
+    src.id = d.id;
+    const double* f[sph::FF_COUNT] = {d.rho, d.p, d.c, d.m, d.gap, d.T, d.kappa, d.cp};
+    for (int k = 0; k < sph::FF_COUNT; ++k) src.field[k] = f[k];
+    src.start = h->sc.start;
+    src.cell_lo = R.dev.cell_off;
+    src.cell_hi = R.dev.cell_off + R.dev.ncells;
+    src.n_upper = std::min<int64_t>(h->n_upper, h->cap);
+    int rc = h->out->enqueue(h->stream, src, file_step, time, err);
+    if (rc != SPH_OK) return fail(h, rc, err);
+    return SPH_OK;
+}
+
+int32_t sph_output_flush(SphHandle* h) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->out) return SPH_OK;
+    std::string err;
+    int rc = h->out->flush(err);
+    if (rc != SPH_OK) return fail(h, rc, err);
+    return SPH_OK;
+}
+
 int32_t sph_destroy(SphHandle* h) {
     if (!h) return SPH_OK;
+    if (h->out) {
+        std::string err;
+        h->out->flush(err);
+        delete h->out;
+        h->out = nullptr;
+    }
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : h->allocs) cudaFree(p);

@@ -195,6 +195,23 @@ class Simulation:
         self._check(self.lib.sph_get_stream(self.h, C.byref(s)))
         return s.value or 0
 
+    # -- VTP output staged off the step stream (sph_output_*)
+    def output_open(self, vtp_io, wall_time: str | None = None) -> None:
+        """Write files of `vtp_io` (VTPIO) from the library: sph_output_write copies the
+        state on the device and a host thread writes the file while later steps run."""
+        syms = (C.c_char_p * max(1, len(vtp_io.field_symbols_)))(*[s.encode() for s in vtp_io.field_symbols_])
+        names = (C.c_char_p * max(1, len(vtp_io.field_names_)))(*[s.encode() for s in vtp_io.field_names_])
+        self._check(self.lib.sph_output_open(self.h, vtp_io.dir_path_.encode(), vtp_io.file_name_.encode(),
+                                             vtp_io.file_suffix_.encode(), vtp_io.step_digit_,
+                                             len(vtp_io.field_symbols_), syms, names,
+                                             None if wall_time is None else wall_time.encode()))
+
+    def output_write(self, file_step: int, time: float) -> None:
+        self._check(self.lib.sph_output_write(self.h, file_step, float(time)))
+
+    def output_flush(self) -> None:
+        self._check(self.lib.sph_output_flush(self.h))
+
     def time_stages(self, reps: int = 10) -> dict:
         ms = np.zeros(_abi.NUM_STAGES)
         self._check(self.lib.sph_time_stages(self.h, reps, _abi.dptr(ms)))
@@ -213,14 +230,17 @@ def _variant(walls):
 
 
 def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: int = _abi.PRECISION_FP64,
-          domain_lo=None, domain_hi=None, periodic_x: bool = False, first_step: int = 1, nsteps: int | None = None):
+          domain_lo=None, domain_hi=None, periodic_x: bool = False, first_step: int = 1, nsteps: int | None = None,
+          staged_output: bool = True, wall_time: str | None = None):
     """GPU counterpart of solve!(fluid, walls..., kernel, model, td, vtp_io; check).
 
-    Runs steps first_step .. td.total_step_ (or `nsteps` steps), writes VTP snapshots
-    at output steps when `vtp_io` is given, and leaves the final state in `fluid`.
-    `domain_lo/hi` bound the cell grid (default: the particles' bounding box grown by
-    two cut-off radii; particles leaving it are clamped into the edge cells, which
-    stays exact but slower).
+    Runs steps first_step .. td.total_step_ (or `nsteps` steps), writes VTP files at
+    step 0 and at output steps when `vtp_io` is given (FluidWallSolve.jl:95,133-136),
+    and leaves the final state in `fluid`.  With `staged_output` the library writes the
+    files from device snapshots while the next steps run; otherwise every output step
+    downloads the state and writes the file here.  `domain_lo/hi` bound the cell grid
+    (default: the particles' bounding box grown by two cut-off radii; particles leaving
+    it are clamped into the edge cells, which stays exact but slower).
     """
     *walls, kernel, model, td = args
     for w in walls:
@@ -238,8 +258,12 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
         for w in walls:
             sim.upload_walls(w)
         sim.upload_fluid(fluid)
-        if vtp_io is not None:
-            vtp_io.write(0, 0.0, fluid, walls)
+        staged = vtp_io is not None and staged_output
+        if staged:
+            sim.output_open(vtp_io, wall_time)
+            sim.output_write(0, 0.0)
+        elif vtp_io is not None:
+            vtp_io.write(0, 0.0, fluid, walls, wall_time=wall_time)
         last = td.total_step_ if nsteps is None else first_step + nsteps - 1
         step = first_step
         while step <= last:
@@ -247,10 +271,19 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
             nxt = step
             while nxt < last and not (vtp_io is not None and isOutputStep(nxt, td)):
                 nxt += 1
-            sim.step(step, nxt - step + 1)
+            if staged:
+                _abi.check(sim.lib, sim.h, sim.lib.sph_step_async(sim.h, step, nxt - step + 1))
+            else:
+                sim.step(step, nxt - step + 1)
             step = nxt + 1
             if vtp_io is not None and isOutputStep(nxt, td):
-                sim.download_into(fluid)
-                vtp_io.write(nxt // td.output_interval_, nxt * td.dt_, fluid, walls)
+                if staged:
+                    sim.output_write(nxt // td.output_interval_, nxt * td.dt_)
+                else:
+                    sim.download_into(fluid)
+                    vtp_io.write(nxt // td.output_interval_, nxt * td.dt_, fluid, walls, wall_time=wall_time)
+        if staged:
+            _abi.check(sim.lib, sim.h, sim.lib.sph_synchronize(sim.h))
+            sim.output_flush()
         sim.download_into(fluid)
     return fluid

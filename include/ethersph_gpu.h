@@ -49,7 +49,8 @@ enum {
     SPH_ERR_GRID_OVERFLOW = 5, /* cell grid or capacity too small for the scene     */
     SPH_ERR_TIMEOUT = 6,       /* a bounded wait gave up                            */
     SPH_ERR_STATE = 7,         /* call out of order (e.g. step before upload)       */
-    SPH_ERR_NO_DEVICE = 8      /* no CUDA device / extension not usable             */
+    SPH_ERR_NO_DEVICE = 8,     /* no CUDA device / extension not usable             */
+    SPH_ERR_IO = 9             /* an output file or directory could not be written  */
 };
 
 /* ---- SPHKernel: src/SPHKernel/SmoothKernel/SmoothKernel.jl:15-20 ------------------ */
@@ -306,6 +307,34 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * form depend on the lane count (the order of the compensated partial sums; -1 sums like
  * 1), never on the block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
+
+/* ---- VTP output without stalling the steps --------------------------------------
+ * Counterpart of writeVTP(step, t, vtp_io, [fluid, walls...]) (src/DataIO/VTPIO.jl:41-98)
+ * as solve! calls it at step 0 and at every output step (FluidWallSolve.jl:95,133-136).
+ * sph_output_write stages the live fluid with device-to-device copies ordered after the
+ * steps already enqueued, then copies it to pinned host memory on a second stream and
+ * writes the file on a host thread while later steps run.  Single-scene handles only.
+ *
+ * sph_output_open: VTPIO's fields (VTPIO.jl:8-15): files are
+ * dir_path/file_name<file_step zero-padded to step_digit><file_suffix>; dir_path is
+ * created if missing (assureDirPathExist, DataIO.jl:35-40).  field_symbols name particle
+ * fields ("rho_", "p_", "c_", "mass_", "gap_", "t_", "kappa_", "cp_"; a leading ':' is
+ * ignored); a symbol a group's particle type lacks gives NaN for that group, as
+ * getParticleFields! (VTPIO.jl:21-38); vector and accumulator fields (x_vec_, drho_, ...)
+ * are SPH_ERR_ARG.  wall_time: fixed WallTime text for every file, or NULL for the
+ * clock.  Groups: the fluid (Type 1), then each sph_upload_walls call in call order
+ * (Type 2, 3, ...).  Files use the VTK XML appended raw layout with UInt64 headers. */
+int32_t sph_output_open(SphHandle* h, const char* dir_path, const char* file_name, const char* file_suffix,
+                        int32_t step_digit, int32_t n_fields, const char* const* field_symbols,
+                        const char* const* field_names, const char* wall_time);
+
+/* Queue the file of file_step (Step field data) at time `time` (Time field data) for
+ * the state after every step enqueued so far.  Returns once the staging copies are
+ * enqueued; waits only when two earlier files are still being written. */
+int32_t sph_output_write(SphHandle* h, int64_t file_step, double time);
+
+/* Wait until every queued file is on disk; returns the first write error (SPH_ERR_IO). */
+int32_t sph_output_flush(SphHandle* h);
 
 /* Text of the last error on this handle (or of the last failed sph_create when h is NULL). */
 const char* sph_last_error(const SphHandle* h);

@@ -97,3 +97,42 @@ def test_vtp_writer_roundtrip(tmp_path, pkg):
     # walls have no density field and no velocity: NaN, as writeVTP writes them
     assert np.all(np.isnan(a["Density"][s.n_fluid:])) and np.all(np.isnan(a["Velocity"][s.n_fluid:]))
     assert a["Step"][0] == 3 and a["Time"][0] == 0.25
+    assert a["WallTime"].count("__") == 1 and len(a["WallTime"]) == len("yyyy/mm/dd__HH:MM:SS.SS")
+
+
+def test_vtp_layout_is_well_formed_xml(tmp_path, pkg):
+    # the header parses as XML, every offset points at a UInt64 size header whose
+    # payload ends where the next one starts, and the block ends the file
+    import xml.etree.ElementTree as ET
+    from ethersph_gb300 import scenes, vtp
+    s = scenes.lid_driven_cavity_2d(n=12)
+    io = vtp.VTPIO(2, "lid_", ".vtp", str(tmp_path), ["rho_", "gap_", "t_"], ["Density", "Gap", "T<&>"])
+    path = io.write(7, 1.5, s.fluid, s.walls, wall_time="2026/01/02__03:04:05.05")
+    raw = open(path, "rb").read()
+    mark = raw.index(b'<AppendedData encoding="raw">')
+    base = raw.index(b"_", mark) + 1
+    root = ET.fromstring(raw[:mark] + b"</VTKFile>")
+    arrays = root.iter("DataArray")
+    offs = sorted(int(a.get("offset")) for a in arrays)
+    pos = 0
+    for o in offs:
+        assert o == pos
+        size = int(np.frombuffer(raw, dtype=np.uint64, count=1, offset=base + o)[0])
+        pos = o + 8 + size
+    assert raw[base + pos:] == b"\n  </AppendedData>\n</VTKFile>\n"
+    a = vtp.read_vtp_arrays(path)
+    nf, n = s.n_fluid, s.n_fluid + s.n_wall
+    assert a["WallTime"] == "2026/01/02__03:04:05.05"
+    # static-velocity walls carry their velocity; no group has t_ here; gap_ everywhere
+    assert np.array_equal(a["Velocity"][nf:], s.walls[0].v_vec_)
+    assert np.all(np.isnan(a["T<&>"])) and np.all(np.isfinite(a["Gap"]))
+    assert np.array_equal(a["connectivity"], np.arange(n)) and np.array_equal(a["offsets"], np.arange(1, n + 1))
+
+
+def test_vtp_rejects_non_scalar_fields(tmp_path, pkg):
+    from ethersph_gb300 import scenes, vtp
+    s = scenes.dam_break_2d(dx=0.1)
+    for bad in ("x_vec_", ":drho_", "sum_kernel_weight_"):
+        io = vtp.VTPIO(1, "d_", ".vtp", str(tmp_path), [bad], ["X"])
+        with pytest.raises(ValueError):
+            io.write(0, 0.0, s.fluid, s.walls)
