@@ -1296,6 +1296,8 @@ int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
             return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
     if (shape[3] < 32 || shape[3] > 1024 || shape[3] % 32 != 0)
         return fail(h, SPH_ERR_ARG, "block size must be a multiple of 32 in [32, 1024]");
+    if (shape[1] == -1 && shape[3] > 256)
+        return fail(h, SPH_ERR_ARG, "the pipelined momentum walk (-1) takes blocks of at most 256 threads");
     for (int k = 0; k < 4; ++k) h->tune[k] = shape[k];
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();

@@ -303,9 +303,11 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 /* Set the FP32 launch shape by hand: shape[4] = (continuity lanes, momentum lanes,
  * Shepard lanes, block size); lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
  * is software-pipelined: loads of the next neighbour overlap the current one's
- * arithmetic), block in {32, 64, ..., 1024} and a multiple of 32.  Results of the FP32
- * form depend on the lane count (the order of the compensated partial sums; -1 sums like
- * 1), never on the block size. */
+ * arithmetic; momentum lanes -1 take blocks of at most 256), block in {32, 64, ..., 1024}
+ * and a multiple of 32.  Results of the FP32
+ * form depend on the lanes code (the order of the compensated partial sums, and for -1
+ * against 1 the compiler's contraction of a*b+c into fused multiply-adds), never on the
+ * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
 
 /* ---- VTP output without stalling the steps --------------------------------------

@@ -216,6 +216,12 @@ def test_errors_are_reported(pkg):
         with pytest.raises(_abi.SphError) as e:
             sim.step(1, 2)
         assert e.value.code == 4  # SPH_ERR_NAN
+    with pkg.Simulation(s.params(precision=1), s.n_fluid, s.n_wall) as sim:
+        for bad_shape in ((3, 1, 1, 128), (1, 1, 1, 48), (1, 1, 1, 2048), (1, -1, 1, 512)):
+            with pytest.raises(_abi.SphError) as e:
+                sim.set_launch_shape(*bad_shape)
+            assert e.value.code == 1  # SPH_ERR_ARG
+        sim.set_launch_shape(1, -1, 1, 256)
     with pytest.raises(_abi.SphError):
         pkg.Simulation(s.params(), 10, 0).upload_fluid(s.fluid)  # capacity overflow
     bad = s.params()
