@@ -21,6 +21,10 @@ ERRORS = {
     5: "SPH_ERR_GRID_OVERFLOW", 6: "SPH_ERR_TIMEOUT", 7: "SPH_ERR_STATE", 8: "SPH_ERR_NO_DEVICE",
     9: "SPH_ERR_IO",
 }
+# probe field codes (SPH_PROBE_*), by particle field symbol and by VTP column name
+PROBE_FIELDS = {"rho_": 0, "p_": 1, "c_": 2, "vx": 3, "vy": 4, "vz": 5, "t_": 6, "mass_": 7,
+                "Density": 0, "Pressure": 1, "SoundSpeed": 2, "VelocityX": 3, "VelocityY": 4, "VelocityZ": 5,
+                "Temperature": 6, "Mass": 7}
 KERNELS = {"CubicSpline": 0, "Gaussian": 1, "WendlandC2": 2, "WendlandC4": 3}
 SOLVE_FLUID_WALL = 0
 SOLVE_FLUID_THERMOSTATIC_WALL = 1
@@ -80,6 +84,8 @@ SIGNATURES = {
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
     "sph_output_open": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
                                     C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_char_p]),
+    "sph_probe": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_double,
+                              C.c_void_p]),
     "sph_output_write": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),
     "sph_output_flush": (C.c_int32, [C.c_void_p]),
     "sph_count_pairs_noalloc": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,

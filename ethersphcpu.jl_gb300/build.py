@@ -3,6 +3,7 @@
 Compiles every translation unit of ``csrc/`` with nvcc in parallel and links
 ``lib/libethersph_gpu.so``.  Per-unit flags:
   sph_fp64.cu  -fmad=false            (plain FP64 path: no a*b+c contraction)
+  sph_probe.cu -fmad=false            (FP64 interpolation, same rounding as the oracle)
   sph_api.cu   -ffp-contract=off      (host constants round like the device code)
 """
 from __future__ import annotations
@@ -24,6 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
           "-Xcompiler", "-Wall", "-I", str(PKG.parent / "include")]
 UNIT_FLAGS = {
     "sph_fp64.cu": ["-fmad=false"],
+    "sph_probe.cu": ["-fmad=false"],
     "sph_api.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 

@@ -298,6 +298,8 @@ struct SphHandle {
     // graph cache: key = (parity, pattern of Shepard steps) -> executable graph
     std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
     sph::VtpWriter* out = nullptr;  // VTP output (sph_output_open)
+    double* probe_buf = nullptr;    // device points + results of sph_probe
+    int64_t probe_cap = 0;          // doubles in probe_buf
     int64_t out_walls = -1;         // wall groups the writer holds
 };
 
@@ -1377,8 +1379,57 @@ int32_t sph_output_flush(SphHandle* h) {
     return SPH_OK;
 }
 
+int32_t sph_probe(SphHandle* h, int64_t n_points, const double* points, int32_t n_fields, const int32_t* fields,
+                  double none_value, double* out) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "probes are for single-scene handles");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_probe before sph_upload_fluid");
+    if (n_points < 0 || n_fields < 1 || n_fields > sph::kMaxProbeFields || !fields ||
+        (n_points > 0 && (!points || !out)))
+        return fail(h, SPH_ERR_ARG, "sph_probe: invalid arguments (1 to 8 fields)");
+    sph::ProbeFields F{};
+    F.n = n_fields;
+    for (int f = 0; f < n_fields; ++f) {
+        const int code = fields[f];
+        if (code < SPH_PROBE_DENSITY || code > SPH_PROBE_MASS) return fail(h, SPH_ERR_ARG, "unknown probe field");
+        if (code == SPH_PROBE_VELOCITY_Z && h->dim != 3) return fail(h, SPH_ERR_ARG, "VELOCITY_Z needs a 3D scene");
+        if (code == SPH_PROBE_TEMPERATURE && !h->thermal)
+            return fail(h, SPH_ERR_ARG, "TEMPERATURE needs a thermal model");
+        F.code[f] = code;
+    }
+    if (n_points == 0) return SPH_OK;
+    const int64_t need = n_points * (h->dim + n_fields);
+    cudaStream_t st = h->stream;
+    if (need > h->probe_cap) {
+        if (h->probe_buf) {
+            SPH_CUDA(h, cudaStreamSynchronize(st));
+            cudaFree(h->probe_buf);
+            h->probe_buf = nullptr;
+            h->probe_cap = 0;
+        }
+        SPH_CUDA(h, cudaMalloc(&h->probe_buf, sizeof(double) * (size_t)need));
+        h->probe_cap = need;
+    }
+    double* d_pts = h->probe_buf;
+    double* d_out = h->probe_buf + n_points * h->dim;
+    SPH_CUDA(h, cudaMemcpyAsync(d_pts, points, sizeof(double) * (size_t)(n_points * h->dim), cudaMemcpyHostToDevice,
+                                st));
+    LaunchCtx L = make_ctx(h);
+    sph::launch_probe(L, n_points, d_pts, F, none_value, d_out);
+    SPH_CUDA(h, cudaGetLastError());
+    SPH_CUDA(h, cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)(n_points * n_fields), cudaMemcpyDeviceToHost,
+                                st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
 int32_t sph_destroy(SphHandle* h) {
     if (!h) return SPH_OK;
+    if (h->probe_buf) {
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        cudaFree(h->probe_buf);
+        h->probe_buf = nullptr;
+    }
     if (h->out) {
         std::string err;
         h->out->flush(err);

@@ -50,6 +50,17 @@ void launch_count_pairs(const LaunchCtx& L, unsigned long long* d_counts);
 
 int scan_max_cells();
 
+// Fields interpolated by launch_probe (SPH_PROBE_* codes), at most kMaxProbeFields.
+constexpr int kMaxProbeFields = 8;
+struct ProbeFields {
+    int n;
+    int code[kMaxProbeFields];
+};
+// SPH interpolation of fluid fields of scene 0 at np device points (dim x np packed)
+// into out (n_fields x np), device arrays.
+void launch_probe(const LaunchCtx& L, int64_t np, const double* pts, const ProbeFields& F, double none_value,
+                  double* out);
+
 }  // namespace sph
 
 #include <string>

@@ -195,6 +195,19 @@ class Simulation:
         self._check(self.lib.sph_get_stream(self.h, C.byref(s)))
         return s.value or 0
 
+    # -- SPH interpolation at points (sph_probe)
+    def probe(self, points, fields=("rho_",), none_value: float = math.nan) -> np.ndarray:
+        """kernelValueInterpolation (VTPToDataFrame.jl:93-142) of the fluid on the
+        device: points (n, dim); fields: particle symbols (rho_, p_, c_, t_, mass_,
+        vx, vy, vz) or VTP column names (Density, VelocityX, ...).  Returns
+        (len(fields), n)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, self.dim)
+        codes = (C.c_int32 * len(fields))(*[_abi.PROBE_FIELDS[str(f).lstrip(":")] for f in fields])
+        out = np.empty((len(fields), len(pts)))
+        self._check(self.lib.sph_probe(self.h, len(pts), pts.ctypes.data, len(fields), codes, float(none_value),
+                                       out.ctypes.data))
+        return out
+
     # -- VTP output staged off the step stream (sph_output_*)
     def output_open(self, vtp_io, wall_time: str | None = None) -> None:
         """Write files of `vtp_io` (VTPIO) from the library: sph_output_write copies the
@@ -287,3 +300,9 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
             sim.output_flush()
         sim.download_into(fluid)
     return fluid
+
+
+def kernelValueInterpolation(points, sim: Simulation, field, none_value: float = math.nan) -> np.ndarray:
+    """Reference-named form of Simulation.probe for one field (VTPToDataFrame.jl:122-142):
+    the interpolated values at `points` (n, dim) from the live fluid of `sim`."""
+    return sim.probe(points, (field,), none_value)[0]

@@ -310,6 +310,28 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
 
+/* ---- SPH interpolation at points (probes) --------------------------------------
+ * kernelValueInterpolation (src/DataIO/VTPToDataFrame.jl:93-142) on the device state:
+ * for each point, f = sum W m_j/rho_j f_j / sum W m_j/rho_j over the fluid particles j
+ * within r_cut (none_value where no particle is in range).  The reference evaluates it
+ * on VTP files after a run; here it reads the live state of a single-scene handle.
+ * points: dim x n_points (host); fields: n_fields codes (1..8) from the list below;
+ * out: n_fields x n_points (host), field-major.  A periodic x axis takes the nearest
+ * image.  SPH_ERR_ARG for an unknown code, VELOCITY_Z in 2D or TEMPERATURE without a
+ * thermal model. */
+enum {
+    SPH_PROBE_DENSITY = 0,     /* rho_ */
+    SPH_PROBE_PRESSURE = 1,    /* p_   */
+    SPH_PROBE_SOUND_SPEED = 2, /* c_   */
+    SPH_PROBE_VELOCITY_X = 3,  /* v_vec_[1] */
+    SPH_PROBE_VELOCITY_Y = 4,  /* v_vec_[2] */
+    SPH_PROBE_VELOCITY_Z = 5,  /* v_vec_[3] (3D) */
+    SPH_PROBE_TEMPERATURE = 6, /* t_ (thermal models) */
+    SPH_PROBE_MASS = 7         /* mass_ */
+};
+int32_t sph_probe(SphHandle* h, int64_t n_points, const double* points, int32_t n_fields, const int32_t* fields,
+                  double none_value, double* out);
+
 /* ---- VTP output without stalling the steps --------------------------------------
  * Counterpart of writeVTP(step, t, vtp_io, [fluid, walls...]) (src/DataIO/VTPIO.jl:41-98)
  * as solve! calls it at step 0 and at every output step (FluidWallSolve.jl:95,133-136).

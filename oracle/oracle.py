@@ -58,6 +58,9 @@ def lib() -> C.CDLL:
         L.or_cell_keys.argtypes = [C.c_void_p, C.c_int64, _DP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.or_neighbour_counts.argtypes = [C.c_void_p, C.c_int64, _DP, C.c_int64, _DP, C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]
+        L.or_probe.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int64, _DP, C.c_int64, _DP,
+                               _DP, _DP, C.c_int, C.POINTER(_DP), C.c_double, _DP]
+        L.or_probe.restype = C.c_int
         L.or_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int64)] + [_DP] * 10 + \
             [C.c_int64] + [_DP] * 6 + [C.POINTER(C.c_int32), C.c_int64, C.c_int64]
         _lib = L
@@ -155,6 +158,23 @@ def run(params, fluid: dict, walls: dict | None, first_step: int, nsteps: int, m
         raise RuntimeError("oracle rejected the parameter block")
     m = n_io.value
     return {k: a[:m] for k, a in st.items()}
+
+
+def probe(kind, dim, rc, points, x, mass, rho, fields, none_value=float("nan"), periodic_x=False, period=0.0):
+    """kernelValueInterpolation restated (brute force, FP64): fields is a list of
+    per-particle arrays; returns an array (len(fields), len(points))."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    xs = np.ascontiguousarray(x, dtype=np.float64)
+    m = np.ascontiguousarray(mass, dtype=np.float64)
+    r = np.ascontiguousarray(rho, dtype=np.float64)
+    fs = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
+    arr = (_DP * max(1, len(fs)))(*[_p(f) for f in fs])
+    out = np.empty((len(fs), len(pts)))
+    rc_ = lib().or_probe(kind, dim, rc, int(periodic_x), period, len(pts), _p(pts), len(xs), _p(xs), _p(m), _p(r),
+                         len(fs), arr, none_value, _p(out))
+    if rc_ != 0:
+        raise ValueError("bad kernel")
+    return out
 
 
 def scene_arrays(scene):

@@ -1032,4 +1032,38 @@ int or_run(const SphParams* prm, int mode, int threads, int64_t* n_fluid, double
     return 0;
 }
 
+// kernelValueInterpolation (src/DataIO/VTPToDataFrame.jl:93-142) by brute force over
+// the fluid: for every point i and every particle j with d(i, j)^2 <= rc^2,
+//   kw_i += W m_j / rho_j,  wv_i += W m_j / rho_j * f_j  (VTPToDataFrame.jl:115-120),
+// result wv_i / kw_i, or none_value where kw_i is not > 0 (:132-138).  A periodic x axis
+// takes the nearest image, as the step's pair search does.  fields: n_fields arrays of
+// n values; out: n_fields x np.
+int or_probe(int kind, int dim, double rc, int periodic_x, double period, int64_t np, const double* pts, int64_t n,
+             const double* x, const double* mass, const double* rho, int n_fields, const double* const* fields,
+             double none_value, double* out) {
+    Kern K;
+    if (!make_kernel(kind, dim, rc, &K) || n_fields < 0) return 1;
+    const double rc2 = rc * rc;
+    std::vector<double> wv((size_t)n_fields);
+    for (int64_t i = 0; i < np; ++i) {
+        double kw = 0.0;
+        std::fill(wv.begin(), wv.end(), 0.0);
+        for (int64_t j = 0; j < n; ++j) {
+            double rv[3];
+            for (int k = 0; k < dim; ++k) rv[k] = pts[i * dim + k] - x[j * dim + k];
+            if (periodic_x) {
+                if (rv[0] > 0.5 * period) rv[0] -= period;
+                else if (rv[0] < -0.5 * period) rv[0] += period;
+            }
+            const double d2 = dist2(rv, dim);
+            if (!(d2 <= rc2)) continue;
+            const double t = kernel_value(std::sqrt(d2), K) * mass[j] / rho[j];
+            kw += t;
+            for (int f = 0; f < n_fields; ++f) wv[(size_t)f] += t * fields[f][j];
+        }
+        for (int f = 0; f < n_fields; ++f) out[f * np + i] = kw > 0.0 ? wv[(size_t)f] / kw : none_value;
+    }
+    return 0;
+}
+
 }  // extern "C"

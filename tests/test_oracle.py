@@ -310,3 +310,56 @@ def test_cell_subdivisions_enumerate_the_same_pairs(pkg, orc):
         rb = orc.run(s.params(cell_subdivision=2), fluid, walls, 1, 6, mode=orc.GATHER, threads=2)
         for k in ("x", "v", "rho"):
             assert _rel(ra[k], rb[k]) < 1e-12, k
+
+
+# ---------------------------------------------------------------- probe interpolation
+def _probe_numpy(orc, kind, dim, rc, pts, x, m, rho, fields, none_value, period=0.0):
+    # kernelValueInterpolation (VTPToDataFrame.jl:93-142) restated with Python loops
+    out = np.full((len(fields), len(pts)), none_value)
+    for i, p in enumerate(pts):
+        kw, wv = 0.0, [0.0] * len(fields)
+        for j in range(len(x)):
+            rv = p - x[j]
+            if period:
+                rv[0] = rv[0] - period if rv[0] > period / 2 else (rv[0] + period if rv[0] < -period / 2 else rv[0])
+            d2 = float(sum(rv[k] * rv[k] for k in range(dim)))
+            if d2 > rc * rc:
+                continue
+            t = orc.kernel_value(kind, dim, rc, math.sqrt(d2)) * m[j] / rho[j]
+            kw += t
+            for f in range(len(fields)):
+                wv[f] += t * fields[f][j]
+        if kw > 0:
+            out[:, i] = [w / kw for w in wv]
+    return out
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_probe_oracle_matches_python_restatement(orc, dim):
+    rng = np.random.default_rng(7)
+    n, rc = 300, 0.3
+    x = rng.uniform(0, 1, (n, dim))
+    m = rng.uniform(0.5, 1.5, n)
+    rho = rng.uniform(900, 1100, n)
+    f1, f2 = rng.normal(size=n), x[:, 0] * 2.0 + 1.0
+    pts = rng.uniform(-0.2, 1.2, (40, dim))
+    got = orc.probe(2, dim, rc, pts, x, m, rho, [f1, f2], none_value=-7.0)
+    ref = _probe_numpy(orc, 2, dim, rc, pts, x, m, rho, [f1, f2], -7.0)
+    assert np.allclose(got, ref, rtol=1e-13, atol=0)
+    far = orc.probe(2, dim, rc, np.full((1, dim), 10.0), x, m, rho, [f1], none_value=-7.0)
+    assert far[0, 0] == -7.0  # no particle in range: none_value (VTPToDataFrame.jl:132-138)
+
+
+def test_probe_oracle_reproduces_constants_and_wraps(orc):
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0, 1, (400, 2))
+    m, rho = np.full(400, 2.0), rng.uniform(1, 2, 400)
+    pts = rng.uniform(0.2, 0.8, (30, 2))
+    c = orc.probe(0, 2, 0.2, pts, x, m, rho, [np.full(400, 3.25)])
+    assert np.allclose(c, 3.25, rtol=1e-14)  # Shepard-normalised: constants are exact
+    # periodic x: a point at x = 0.01 sees particles near x = 0.99 through the wrap
+    edge = np.array([[0.01, 0.5]])
+    plain = orc.probe(0, 2, 0.2, edge, x, m, rho, [x[:, 0]])
+    wrapped = orc.probe(0, 2, 0.2, edge, x, m, rho, [x[:, 0]], periodic_x=True, period=1.0)
+    ref = _probe_numpy(orc, 0, 2, 0.2, edge, x, m, rho, [x[:, 0]], float("nan"), period=1.0)
+    assert np.allclose(wrapped, ref, rtol=1e-13) and wrapped[0, 0] > plain[0, 0]
