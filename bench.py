@@ -36,6 +36,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle-steps/s"
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) of one momentum launch on the default workload, measured with
+# ncu --set full --clock-control none (cold L2, as the bench's flushed steps)
+MOMENTUM_DRAM_BYTES_256 = 7.610112e6
 
 
 def parse():
@@ -171,15 +174,18 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- our arm
 def algorithmic_bytes(scene, precision):
-    """Bytes each particle's SoA elements move through the momentum kernel (read or
-    written once) for one launch: the unit of roofline.achieved."""
+    """Bytes the momentum kernel must move for one launch on the 2D thermal cavity (each
+    per-particle SoA element it reads or writes, once; neighbour re-reads count zero):
+    the numerator of roofline.achieved."""
     nf, nw = scene.n_fluid, scene.n_wall
+    assert scene.fluid.x_vec_.shape[1] == 2 and scene.fluid.thermal
+    writes = 16 + 16 + 8 + 8 + 4 + 4  # x' v' (double2) T' rho' key slot
     if precision == "fp64":
-        fluid = (16 + 16 + 8 * 8) + (16 + 16 + 8 + 8 + 4 + 4)  # x v rhoc P m gap c T kappa cp | x' v' T' rho' key slot
-        wall = 16 + 16 + 16 + 8 + 8 + 8 + 4                    # x n v gap T kappa kind
+        fluid = (16 + 16 + 8 * 8 + 4) + writes  # x v | rhoc P m gap c T kappa cp | scene
+        wall = 16 + 16 + 16 + 8 + 8 + 8 + 4     # x n v gap T kappa kind
     else:
-        fluid = (16 + 16 + 16) + (16 + 16 + 8 + 8 + 4 + 4)   # float4 shadows | FP64 masters out
-        wall = 16 + 16 + 16
+        fluid = (16 + 16 + 16 + 8 + 4 + 4 + 16 + 16 + 8 + 8) + writes  # fa fb fc c cell scene | x v T rhoc
+        wall = 16 + 16 + 16                                           # float4 shadows fa fb fc
     return nf * fluid + nw * wall
 
 
@@ -344,9 +350,12 @@ def run_ours(args, rank, world, local):
             "frac": achieved / hbm,
             "peak_source": f"{peak_src} hbm_gbs",
             "algorithmic_bytes_per_launch": bytes_mom,
-            "traffic": None,
-            "note": "FP64 pair arithmetic is ALU-bound on GB300; the HBM fraction is low by design"
-            if args.precision == "fp64" else "",
+            "traffic": MOMENTUM_DRAM_BYTES_256 if (args.n == 256 and args.precision == "fp32c") else None,
+            "traffic_source": "ncu --set full of this launch at n=256, shape -1,-1,-1,128: "
+                              "dram__bytes_read.sum + dram__bytes_write.sum",
+            "note": ("FP64 pair arithmetic is ALU-bound on GB300 (FP64 at 1/64 of the FP32 rate)"
+                     if args.precision == "fp64" else
+                     "issue/latency-bound: dependent neighbour loads and pair arithmetic, not bytes"),
         },
         "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
