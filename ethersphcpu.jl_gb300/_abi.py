@@ -84,6 +84,7 @@ SIGNATURES = {
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
     "sph_output_open": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
                                     C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_char_p]),
+    "sph_scene_footprint": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_int64, C.POINTER(C.c_int64)]),
     "sph_probe": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_double,
                               C.c_void_p]),
     "sph_output_write": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),

@@ -1112,6 +1112,23 @@ int32_t sph_batch_retire(SphHandle* h, int32_t scene_id) {
     return SPH_OK;
 }
 
+int32_t sph_scene_footprint(const SphParams* params, int64_t n_fluid, int64_t n_wall, int64_t* out) {
+    if (!params || !out || n_fluid < 0 || n_wall < 0) {
+        set_global_error("sph_scene_footprint: invalid arguments");
+        return SPH_ERR_ARG;
+    }
+    SceneDev S{};
+    std::string err;
+    if (!build_scene(*params, S, err)) {
+        set_global_error(err);
+        return SPH_ERR_ARG;
+    }
+    out[0] = n_fluid;
+    out[1] = (int64_t)S.ncells + 1;
+    out[2] = n_wall;
+    return SPH_OK;
+}
+
 int32_t sph_batch_free(SphHandle* h, int64_t* out) {
     if (!h || !out) return fail(h, SPH_ERR_ARG, "null argument");
     int32_t n = 0;

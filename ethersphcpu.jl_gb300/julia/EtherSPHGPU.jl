@@ -13,12 +13,21 @@
   particle is deleted at a check step when a coordinate is > hi or < lo), which is what
   the examples' check functions express (CollapseDry.jl:119-127).  A `check` function
   given without `aabb` is applied on the host at output steps only.
+
+  With `staged_output = true` (the default when no host-side check is needed) the files
+  are written by the library (sph_output_*): the state after an output step is copied on
+  the device and written by a library thread while the next steps run; the files hold
+  the same fields and groups as writeVTP's, in VTK's appended raw layout.
+
+  Also here: `GPUScene` (a device-resident scene: step!, download!, probe via
+  kernelValueInterpolation), `GPUBatch` (many scenes stepped together) and `serve`, the
+  request loop that admits scenes by device footprint into running batches.
 =#
 module EtherSPHGPU
 
 using EtherSPHCPU
 
-export GPU, FP64, FP32Compensated
+export GPU, FP64, FP32Compensated, GPUScene, GPUBatch, SceneRequest, serve, step!, download!, probe
 
 const libsph = joinpath(@__DIR__, "..", "lib", "libethersph_gpu.so")
 
@@ -74,6 +83,11 @@ wallCode(::StaticVelocityWallParticle) = Int32(1)
 wallCode(::ThermostaticWallParticle) = Int32(2)
 
 pad3(v) = ntuple(k -> k <= length(v) ? Float64(v[k]) : 0.0, 3)
+
+# solve variant of a wall group (SPH_SOLVE_*): FluidWallSolve, FluidThermostaticWallSolve,
+# FluidVelocitySolve
+solveCode(walls) = walls[1] isa ThermostaticWallParticle ? Int32(1) :
+                   walls[1] isa StaticVelocityWallParticle ? Int32(3) : Int32(0)
 isThermal(m) = m isa ThermalWeaklyCompressibleLiquidModel
 
 function makeParams(kernel, model, td, solve_code, precision, aabb, domain, periodic_x)
@@ -95,7 +109,7 @@ function makeParams(kernel, model, td, solve_code, precision, aabb, domain, peri
     )
 end
 
-function check(h, rc)
+function checkStatus(h, rc)
     if rc != 0
         msg = unsafe_string(ccall((:sph_last_error, libsph), Cstring, (Ptr{Cvoid},), h))
         error("EtherSPHGPU error $rc: $msg")
@@ -110,7 +124,7 @@ function uploadFluid(h, fluid)
     sc(f) = Float64[getfield(p, f) for p in fluid]
     th = fluid[1] isa ThermalLiquidParticle
     t, kappa, cp = th ? (sc(:t_), sc(:kappa_), sc(:cp_)) : (C_NULL, C_NULL, C_NULL)
-    check(h, ccall((:sph_upload_fluid, libsph), Int32,
+    checkStatus(h, ccall((:sph_upload_fluid, libsph), Int32,
         (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
          Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
         h, length(fluid), x, v, sc(:rho_), sc(:p_), sc(:c_), sc(:mass_), sc(:gap_), t, kappa, cp))
@@ -124,7 +138,7 @@ function uploadWalls(h, walls)
     t = kind == 2 ? Float64[w.t_ for w in walls] : C_NULL
     kappa = kind == 2 ? Float64[w.kappa_ for w in walls] : C_NULL
     v = kind == 1 ? stack(walls, :v_vec_) : C_NULL
-    check(h, ccall((:sph_upload_walls, libsph), Int32,
+    checkStatus(h, ccall((:sph_upload_walls, libsph), Int32,
         (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
         h, kind, length(walls), x, n, gap, t, kappa, v))
 end
@@ -138,12 +152,12 @@ function downloadFluid!(h, fluid)
     th = fluid[1] isa ThermalLiquidParticle
     t = th ? zeros(cap) : C_NULL
     n = Ref{Int64}(0)
-    check(h, ccall((:sph_download_fluid, libsph), Int32,
+    checkStatus(h, ccall((:sph_download_fluid, libsph), Int32,
         (Ptr{Cvoid}, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
          Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
         h, cap, n, x, v, rho, p, c, m, gap, t, C_NULL, C_NULL))
     ids = zeros(Int64, cap)
-    check(h, ccall((:sph_download_ids, libsph), Int32, (Ptr{Cvoid}, Int64, Ref{Int64}, Ptr{Int64}), h, cap, n, ids))
+    checkStatus(h, ccall((:sph_download_ids, libsph), Int32, (Ptr{Cvoid}, Int64, Ref{Int64}, Ptr{Int64}), h, cap, n, ids))
     keep = falses(cap)
     keep[ids[1:n[]] .+ 1] .= true
     deleteat!(fluid, findall(.!keep))
@@ -158,8 +172,21 @@ function downloadFluid!(h, fluid)
     return nothing
 end
 
+function openOutput(h, vtp_io::VTPIO)
+    syms = [lstrip(String(x), ':') for x in vtp_io.field_symbols_]
+    names = String[x for x in vtp_io.field_names_]
+    checkStatus(h, ccall((:sph_output_open, libsph), Int32,
+        (Ptr{Cvoid}, Cstring, Cstring, Cstring, Int32, Int32, Ptr{Cstring}, Ptr{Cstring}, Cstring),
+        h, vtp_io.dir_path_, vtp_io.file_name_, vtp_io.file_suffix_, Int32(vtp_io.step_digit_), Int32(length(syms)),
+        syms, names, C_NULL))
+end
+
+outputWrite(h, file_step, t) =
+    checkStatus(h, ccall((:sph_output_write, libsph), Int32, (Ptr{Cvoid}, Int64, Float64), h, file_step, t))
+outputFlush(h) = checkStatus(h, ccall((:sph_output_flush, libsph), Int32, (Ptr{Cvoid},), h))
+
 function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, check, aabb, precision, domain,
-    periodic_x)
+    periodic_x, staged_output)
     if domain === nothing
         pts = reduce(hcat, [stack(g, :x_vec_) for g in [[fluid]; wall_groups] if !isempty(g)])
         pad = 2 * kernel.influence_radius_
@@ -168,32 +195,43 @@ function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, ch
     prm = Ref(makeParams(kernel, model, td, solve_code, precision, aabb, domain, periodic_x))
     h = Ref{Ptr{Cvoid}}(C_NULL)
     nw = sum(length, wall_groups; init = 0)
-    check(C_NULL, ccall((:sph_create, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ref{Ptr{Cvoid}}),
+    checkStatus(C_NULL, ccall((:sph_create, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ref{Ptr{Cvoid}}),
         prm, length(fluid), nw, h))
+    staged = staged_output && (aabb !== nothing || check === defaultCheck)
     try
         foreach(g -> uploadWalls(h[], g), wall_groups)
         uploadFluid(h[], fluid)
-        assureDirPathExist(vtp_io)
-        writeVTP(0, 0.0, vtp_io, [[fluid]; wall_groups])
+        if staged
+            openOutput(h[], vtp_io)
+            outputWrite(h[], 0, 0.0)
+        else
+            assureDirPathExist(vtp_io)
+            writeVTP(0, 0.0, vtp_io, [[fluid]; wall_groups])
+        end
         step = 1
         while step <= td.total_step_
             last = min(td.total_step_, (div(step - 1, td.output_interval_) + 1) * td.output_interval_)
             try
-                check(h[], ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), h[], step, last - step + 1))
+                checkStatus(h[], ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), h[], step, last - step + 1))
             catch e  # FluidWallSolve.jl:130-134: report and continue
                 println(e)
                 println("Error at step: ", last)
             end
             if isOutputStep(last, td)
-                downloadFluid!(h[], fluid)
-                if aabb === nothing && check !== defaultCheck
-                    deleteat!(fluid, findall(p -> !check(p), fluid))
-                    uploadFluid(h[], fluid)
+                if staged  # the library copies the state and writes while the next steps run
+                    outputWrite(h[], div(last, td.output_interval_), last * td.dt_)
+                else
+                    downloadFluid!(h[], fluid)
+                    if aabb === nothing && check !== defaultCheck
+                        deleteat!(fluid, findall(p -> !check(p), fluid))
+                        uploadFluid(h[], fluid)
+                    end
+                    writeVTP(div(last, td.output_interval_), last * td.dt_, vtp_io, [[fluid]; wall_groups])
                 end
-                writeVTP(div(last, td.output_interval_), last * td.dt_, vtp_io, [[fluid]; wall_groups])
             end
             step = last + 1
         end
+        staged && outputFlush(h[])
         downloadFluid!(h[], fluid)
     finally
         ccall((:sph_destroy, libsph), Int32, (Ptr{Cvoid},), h[])
@@ -207,11 +245,10 @@ function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidPartic
     wall_particles::AbstractVector{<:WallParticle}, smooth_kernel::SmoothKernel,
     wc_lm::WeaklyCompressibleLiquidModel, dr_fti_forward_euler::DensityReinitializedFixedTimeIntervalForwardEuler,
     vtp_io::VTPIO; check::Function = defaultCheck, aabb = nothing, precision = FP64, domain = nothing,
-    periodic_x::Bool = false)::Nothing
-    code = wall_particles[1] isa ThermostaticWallParticle ? Int32(1) :
-           wall_particles[1] isa StaticVelocityWallParticle ? Int32(3) : Int32(0)
+    periodic_x::Bool = false, staged_output::Bool = true)::Nothing
+    code = solveCode(wall_particles)
     return runSolve!(code, fluid_particles, [wall_particles], smooth_kernel, wc_lm, dr_fti_forward_euler, vtp_io,
-        check, aabb, precision, domain, periodic_x)
+        check, aabb, precision, domain, periodic_x, staged_output)
 end
 
 # FluidCompulsiveThermostaticWallSolve.jl:154-233
@@ -220,9 +257,271 @@ function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidPartic
     thermostatic_wall_particles::AbstractVector{<:ThermostaticWallParticle}, smooth_kernel::SmoothKernel,
     th_wc_lm::ThermalWeaklyCompressibleLiquidModel,
     dr_fti_forward_euler::DensityReinitializedFixedTimeIntervalForwardEuler, vtp_io::VTPIO;
-    check::Function = defaultCheck, aabb = nothing, precision = FP64, domain = nothing)::Nothing
+    check::Function = defaultCheck, aabb = nothing, precision = FP64, domain = nothing,
+    staged_output::Bool = true)::Nothing
     return runSolve!(Int32(2), fluid_particles, [wall_particles, thermostatic_wall_particles], smooth_kernel,
-        th_wc_lm, dr_fti_forward_euler, vtp_io, check, aabb, precision, domain, false)
+        th_wc_lm, dr_fti_forward_euler, vtp_io, check, aabb, precision, domain, false, staged_output)
+end
+
+# ---------------------------------------------------------------- a device-resident scene
+"""
+    GPUScene(fluid, wall_groups, kernel, model, td; precision, domain, aabb, periodic_x)
+
+One scene held on the device (sph_create + uploads).  `step!(s, first, n)` runs steps
+first .. first+n-1 of eachStep!; `download!(s, fluid)` copies the live particles back
+(deleteat! for removed ones); `kernelValueInterpolation(points, s, field)` interpolates a
+fluid field at points on the device (VTPToDataFrame.jl:93-142); `close(s)` frees it.
+"""
+mutable struct GPUScene
+    h::Ptr{Cvoid}
+    dim::Int
+end
+
+function GPUScene(fluid, wall_groups, kernel, model, td; precision = FP64, domain = nothing, aabb = nothing,
+    periodic_x::Bool = false)
+    if domain === nothing
+        pts = reduce(hcat, [stack(g, :x_vec_) for g in [[fluid]; wall_groups] if !isempty(g)])
+        pad = 2 * kernel.influence_radius_
+        domain = (vec(minimum(pts; dims = 2)) .- pad, vec(maximum(pts; dims = 2)) .+ pad)
+    end
+    code = isThermal(model) ? (length(wall_groups) > 1 ? Int32(2) : Int32(1)) : solveCode(wall_groups[1])
+    prm = Ref(makeParams(kernel, model, td, code, precision, aabb, domain, periodic_x))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    checkStatus(C_NULL, ccall((:sph_create, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ref{Ptr{Cvoid}}),
+        prm, length(fluid), sum(length, wall_groups; init = 0), h))
+    s = GPUScene(h[], Int(kernel.dim_))
+    foreach(g -> uploadWalls(s.h, g), wall_groups)
+    uploadFluid(s.h, fluid)
+    finalizer(close, s)
+    return s
+end
+
+function Base.close(s::GPUScene)
+    if s.h != C_NULL
+        ccall((:sph_destroy, libsph), Int32, (Ptr{Cvoid},), s.h)
+        s.h = C_NULL
+    end
+    return nothing
+end
+
+step!(s::GPUScene, first_step::Integer, nsteps::Integer) =
+    checkStatus(s.h, ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), s.h, first_step, nsteps))
+download!(s::GPUScene, fluid) = downloadFluid!(s.h, fluid)
+
+const probeCodes = Dict(:rho_ => 0, :p_ => 1, :c_ => 2, :t_ => 6, :mass_ => 7, "Density" => 0, "Pressure" => 1,
+    "SoundSpeed" => 2, "VelocityX" => 3, "VelocityY" => 4, "VelocityZ" => 5, "Temperature" => 6, "Mass" => 7)
+
+"""
+    probe(s::GPUScene, points::Matrix{Float64}, fields; none_value = NaN) -> Matrix
+
+SPH interpolation of fluid fields (symbols such as :rho_ or column names such as
+"VelocityX") at the columns of `points` (dim x n); one row per field.
+"""
+function probe(s::GPUScene, points::AbstractMatrix, fields; none_value::Float64 = NaN)
+    pts = Matrix{Float64}(points)
+    codes = Int32[probeCodes[f] for f in fields]
+    out = zeros(Float64, size(pts, 2), length(codes))  # column-major: out[:, k] is field k
+    checkStatus(s.h, ccall((:sph_probe, libsph), Int32,
+        (Ptr{Cvoid}, Int64, Ptr{Float64}, Int32, Ptr{Int32}, Float64, Ptr{Float64}),
+        s.h, size(pts, 2), pts, Int32(length(codes)), codes, none_value, out))
+    return permutedims(out)
+end
+
+# kernelValueInterpolation(points, view, field, kernel, indices) of VTPToDataFrame.jl,
+# evaluated on the live device state of `s` (fluid particles) instead of a VTP file.
+EtherSPHCPU.kernelValueInterpolation(points::Matrix, s::GPUScene, field; none_value::Float64 = NaN) =
+    vec(probe(s, points, [field]; none_value = none_value))
+
+# ---------------------------------------------------------------- batches and serving
+"""
+    GPUBatch(prototype::SphParams, particles, cells, walls, scenes)
+
+A batch handle (sph_batch_create): scenes of one dim / kernel / solve / form share the
+kernel launches; capacities are the device budget.
+"""
+mutable struct GPUBatch
+    h::Ptr{Cvoid}
+end
+
+function GPUBatch(prototype::SphParams, particles::Integer, cells::Integer, walls::Integer, scenes::Integer)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    checkStatus(C_NULL, ccall((:sph_batch_create, libsph), Int32,
+        (Ref{SphParams}, Int64, Int64, Int64, Int32, Ref{Ptr{Cvoid}}),
+        Ref(prototype), particles, cells, walls, Int32(scenes), h))
+    b = GPUBatch(h[])
+    finalizer(close, b)
+    return b
+end
+
+function Base.close(b::GPUBatch)
+    if b.h != C_NULL
+        ccall((:sph_destroy, libsph), Int32, (Ptr{Cvoid},), b.h)
+        b.h = C_NULL
+    end
+    return nothing
+end
+
+function freeSlots(b::GPUBatch)
+    out = zeros(Int64, 4)
+    checkStatus(b.h, ccall((:sph_batch_free, libsph), Int32, (Ptr{Cvoid}, Ptr{Int64}), b.h, out))
+    return (particles = out[1], cells = out[2], walls = out[3], scenes = out[4])
+end
+
+function footprint(prm::SphParams, n_fluid::Integer, n_wall::Integer)
+    out = zeros(Int64, 3)
+    checkStatus(C_NULL, ccall((:sph_scene_footprint, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ptr{Int64}),
+        Ref(prm), n_fluid, n_wall, out))
+    return (particles = out[1], cells = out[2], walls = out[3])
+end
+
+function addScene!(b::GPUBatch, prm::SphParams, first_step::Integer, nsteps::Integer, fluid, wall_groups)
+    x, v = stack(fluid, :x_vec_), stack(fluid, :v_vec_)
+    sc(f) = Float64[getfield(p, f) for p in fluid]
+    th = fluid[1] isa ThermalLiquidParticle
+    t, kappa, cp = th ? (sc(:t_), sc(:kappa_), sc(:cp_)) : (C_NULL, C_NULL, C_NULL)
+    walls = reduce(vcat, wall_groups; init = WallParticle[])
+    nw = length(walls)
+    kinds = Int32[wallCode(w) for w in walls]
+    wx = nw > 0 ? stack(walls, :x_vec_) : zeros(0, 0)
+    wn = nw > 0 ? stack(walls, :normal_vec_) : zeros(0, 0)
+    wgap = Float64[w.gap_ for w in walls]
+    wt = Float64[w isa ThermostaticWallParticle ? w.t_ : 0.0 for w in walls]
+    wk = Float64[w isa ThermostaticWallParticle ? w.kappa_ : 0.0 for w in walls]
+    dim = length(fluid[1].x_vec_)
+    wv = nw > 0 ? reduce(hcat, [w isa StaticVelocityWallParticle ? collect(Float64, w.v_vec_) : zeros(dim)
+                               for w in walls]) : zeros(0, 0)
+    id = Ref{Int32}(-1)
+    checkStatus(b.h, ccall((:sph_batch_add_scene, libsph), Int32,
+        (Ptr{Cvoid}, Ref{SphParams}, Int64, Int64, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Int32},
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Int32}),
+        b.h, Ref(prm), first_step, nsteps, length(fluid), x, v, sc(:rho_), sc(:p_), sc(:c_), sc(:mass_), sc(:gap_),
+        t, kappa, cp, nw, kinds, wx, wn, wgap, wt, wk, wv, id))
+    return Int(id[])
+end
+
+stepBatch!(b::GPUBatch, nsteps::Integer) =
+    checkStatus(b.h, ccall((:sph_batch_step, libsph), Int32, (Ptr{Cvoid}, Int64), b.h, nsteps))
+synchronize(b::GPUBatch) = checkStatus(b.h, ccall((:sph_synchronize, libsph), Int32, (Ptr{Cvoid},), b.h))
+retire!(b::GPUBatch, id::Integer) =
+    checkStatus(b.h, ccall((:sph_batch_retire, libsph), Int32, (Ptr{Cvoid}, Int32), b.h, Int32(id)))
+
+function downloadScene!(b::GPUBatch, id::Integer, fluid)
+    cap = length(fluid)
+    dim = length(fluid[1].x_vec_)
+    x, v = zeros(dim, cap), zeros(dim, cap)
+    rho, p, c, m, gap = zeros(cap), zeros(cap), zeros(cap), zeros(cap), zeros(cap)
+    th = fluid[1] isa ThermalLiquidParticle
+    t, kappa, cp = th ? (zeros(cap), zeros(cap), zeros(cap)) : (C_NULL, C_NULL, C_NULL)
+    n = Ref{Int64}(0)
+    checkStatus(b.h, ccall((:sph_batch_download_scene, libsph), Int32,
+        (Ptr{Cvoid}, Int32, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        b.h, Int32(id), cap, n, x, v, rho, p, c, m, gap, t, kappa, cp))
+    # the survivors in their original order; every field comes from the device, so the
+    # first n structs are reused whichever particles were deleted
+    resize!(fluid, n[])
+    for (i, pt) in enumerate(fluid)
+        pt.x_vec_ .= view(x, :, i)
+        pt.v_vec_ .= view(v, :, i)
+        pt.rho_ = rho[i]
+        pt.p_ = p[i]
+        pt.c_ = c[i]
+        pt.mass_ = m[i]
+        pt.gap_ = gap[i]
+        if th
+            pt.t_ = t[i]
+            pt.kappa_ = kappa[i]
+            pt.cp_ = cp[i]
+        end
+    end
+    return fluid
+end
+
+"""
+    SceneRequest(t_arrival, fluid, wall_groups, kernel, model, td; precision, domain, aabb, periodic_x)
+
+A scene to serve: it arrives at `t_arrival` seconds and runs td.total_step_ steps.
+"""
+struct SceneRequest
+    t_arrival::Float64
+    fluid::Any
+    wall_groups::Any
+    params::SphParams
+    nsteps::Int
+end
+
+function SceneRequest(t_arrival, fluid, wall_groups, kernel, model, td; precision = FP32Compensated,
+    domain = nothing, aabb = nothing, periodic_x::Bool = false)
+    if domain === nothing
+        pts = reduce(hcat, [stack(g, :x_vec_) for g in [[fluid]; wall_groups] if !isempty(g)])
+        pad = 2 * kernel.influence_radius_
+        domain = (vec(minimum(pts; dims = 2)) .- pad, vec(maximum(pts; dims = 2)) .+ pad)
+    end
+    code = isThermal(model) ? (length(wall_groups) > 1 ? Int32(2) : Int32(1)) : solveCode(wall_groups[1])
+    prm = makeParams(kernel, model, td, code, precision, aabb, domain, periodic_x)
+    return SceneRequest(Float64(t_arrival), fluid, wall_groups, prm, Int(td.total_step_))
+end
+
+"""
+    serve(requests, batches::Dict{Int, GPUBatch}; bundle = 10) -> (results, wall_s, particle_steps)
+
+The request loop: requests (sorted by arrival) join the queue of their dimension when
+they arrive; a queued scene is admitted into its batch as soon as its footprint fits the
+batch's free particle slots, cell run, wall run and scene slot; every bundle advances all
+resident scenes together; finished scenes are downloaded into their fluid vectors and
+retired, which frees room for the queue.  `results` holds (request, t_admit, t_done) with
+times in seconds from the start; latency = t_done - t_arrival.
+"""
+function serve(requests::Vector{SceneRequest}, batches::Dict{Int, GPUBatch}; bundle::Int = 10)
+    pending = sort(requests; by = r -> r.t_arrival)
+    queues = Dict(d => SceneRequest[] for d in keys(batches))
+    active = Dict{Tuple{Int, Int}, Any}()
+    results = Tuple{SceneRequest, Float64, Float64}[]
+    particle_steps = 0
+    t0 = time()
+    while !isempty(pending) || !isempty(active) || any(!isempty, values(queues))
+        now = time() - t0
+        while !isempty(pending) && pending[1].t_arrival <= now
+            r = popfirst!(pending)
+            push!(queues[Int(r.params.dim)], r)
+        end
+        for (dim, q) in queues
+            b = batches[dim]
+            while !isempty(q)
+                r = q[1]
+                need = footprint(r.params, length(r.fluid), sum(length, r.wall_groups; init = 0))
+                fr = freeSlots(b)
+                (need.particles <= fr.particles && need.cells <= fr.cells && need.walls <= fr.walls &&
+                 fr.scenes >= 1) || break
+                popfirst!(q)
+                id = addScene!(b, r.params, 1, r.nsteps, r.fluid, r.wall_groups)
+                active[(dim, id)] = [r, time() - t0, r.nsteps, length(r.fluid)]
+            end
+        end
+        if isempty(active)
+            isempty(pending) || sleep(max(0.0, min(0.01, pending[1].t_arrival - (time() - t0))))
+            continue
+        end
+        running = unique(first.(collect(keys(active))))
+        foreach(d -> stepBatch!(batches[d], bundle), running)
+        foreach(d -> synchronize(batches[d]), running)
+        t_now = time() - t0
+        for key in collect(keys(active))
+            rec = active[key]
+            n = min(bundle, rec[3])
+            particle_steps += n * rec[4]
+            rec[3] -= n
+            if rec[3] <= 0
+                dim, id = key
+                downloadScene!(batches[dim], id, rec[1].fluid)
+                retire!(batches[dim], id)
+                push!(results, (rec[1], rec[2], t_now))
+                delete!(active, key)
+            end
+        end
+    end
+    return results, time() - t0, particle_steps
 end
 
 end # module

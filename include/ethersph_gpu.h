@@ -270,6 +270,11 @@ int32_t sph_batch_download_scene(SphHandle* h, int32_t scene_id, int64_t capacit
 /* Drop a scene's particles and free its slot, cells and walls. */
 int32_t sph_batch_retire(SphHandle* h, int32_t scene_id);
 
+/* What a scene occupies in a batch: out[3] = (fluid particles, cells including the
+ * scene's sentinel cell, wall particles), from the grid the library would build for
+ * `params` (no device needed).  Admission control compares it with sph_batch_free. */
+int32_t sph_scene_footprint(const SphParams* params, int64_t n_fluid, int64_t n_wall, int64_t* out);
+
 /* out[4] = (free particle slots, largest free run of cells, largest free run of walls,
  * free scene slots): what admission control compares a scene's footprint with. */
 int32_t sph_batch_free(SphHandle* h, int64_t* out);

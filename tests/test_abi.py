@@ -136,3 +136,40 @@ def test_vtp_rejects_non_scalar_fields(tmp_path, pkg):
         io = vtp.VTPIO(1, "d_", ".vtp", str(tmp_path), [bad], ["X"])
         with pytest.raises(ValueError):
             io.write(0, 0.0, s.fluid, s.walls)
+
+
+def test_scene_footprint_matches_the_host_model(pkg):
+    # the admission arithmetic of batch.footprint (Python) and sph_scene_footprint (the
+    # library's own grid builder) agree; no device is needed
+    import ctypes as C
+    from ethersph_gb300 import _abi, batch, scenes
+    lib = _abi.load_library()
+    cases = [scenes.dam_break_2d(dx=0.05), scenes.natural_convection_2d(n=40),
+             scenes.poiseuille_periodic_2d(n_across=16), scenes.lid_driven_cavity_2d(n=20),
+             scenes.dam_break_3d(dx=0.05, tank=(0.6, 0.3, 0.4), column=(0.2, 0.2, 0.3))]
+    for s in cases:
+        for prec in (0, 1):
+            out = (C.c_int64 * 3)()
+            _abi.check(lib, None, lib.sph_scene_footprint(C.byref(s.params(precision=prec)), s.n_fluid, s.n_wall,
+                                                          out))
+            assert tuple(out) == batch.footprint(s, prec), (s.name, prec)
+    bad = cases[0].params()
+    bad.dim = 4
+    assert lib.sph_scene_footprint(C.byref(bad), 1, 1, (C.c_int64 * 3)()) == 1
+
+
+def test_julia_binding_names_declared_entry_points_and_fields():
+    # the Julia binding is not run here (no Julia); check it against the header: every
+    # symbol it ccalls is declared, and its SphParams mirror has the C fields in order
+    jl = (ROOT / "ethersphcpu.jl_gb300" / "julia" / "EtherSPHGPU.jl").read_text()
+    called = set(re.findall(r"ccall\(\(:(sph_\w+), libsph\)", jl))
+    assert called and called <= declared_symbols(), called - declared_symbols()
+    assert {"sph_output_open", "sph_output_write", "sph_probe", "sph_batch_add_scene",
+            "sph_scene_footprint"} <= called
+    body = re.search(r"struct SphParams\n(.*?)\nend", jl, flags=re.S).group(1)
+    jl_fields = re.findall(r"^\s*(\w+)::", body, flags=re.M)
+    hdr = (ROOT / "include" / "ethersph_gpu.h").read_text()
+    c_body = re.search(r"typedef struct SphParams \{(.*?)\}\s*SphParams;", hdr, flags=re.S).group(1)
+    c_body = re.sub(r"/\*.*?\*/", "", c_body, flags=re.S)
+    c_fields = re.findall(r"\b(\w+)(?:\[\d\])?\s*;", c_body)
+    assert jl_fields == c_fields
