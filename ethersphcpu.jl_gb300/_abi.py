@@ -30,6 +30,7 @@ SOLVE_FLUID_WALL = 0
 SOLVE_FLUID_THERMOSTATIC_WALL = 1
 SOLVE_FLUID_COMPULSIVE_THERMOSTATIC_WALL = 2
 SOLVE_FLUID_VELOCITY_WALL = 3
+SOLVE_FLUID_INLET_OUTLET_WALL = 4
 WALL_COMPULSIVE = 0
 WALL_STATIC_VELOCITY = 1
 WALL_THERMOSTATIC = 2
@@ -54,6 +55,13 @@ class SphParams(C.Structure):
         ("domain_lo", C.c_double * 3), ("domain_hi", C.c_double * 3),
         ("nan_check", C.c_int32), ("cell_subdivision", C.c_int32),
     ]
+
+
+class SphBufferRules(C.Structure):
+    """SphBufferRules (include/ethersph_gpu.h): the plane tests of the inlet/outlet solve."""
+    _fields_ = [("inlet_normal", C.c_double * 3), ("inlet_offset", C.c_double), ("inlet_shift", C.c_double * 3),
+                ("outlet_normal", C.c_double * 3), ("outlet_offset", C.c_double),
+                ("drop_normal", C.c_double * 3), ("drop_offset", C.c_double)]
 
 
 class SphStats(C.Structure):
@@ -85,6 +93,10 @@ SIGNATURES = {
     "sph_output_open": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,
                                     C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_char_p]),
     "sph_scene_footprint": (C.c_int32, [C.POINTER(SphParams), C.c_int64, C.c_int64, C.POINTER(C.c_int64)]),
+    "sph_upload_buffers": (C.c_int32, [C.c_void_p, C.POINTER(SphBufferRules), C.c_int64, C.c_int64] + [C.c_void_p] * 7
+                           + [C.c_int64] + [C.c_void_p] * 7),
+    "sph_set_buffer_velocity": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p]),
+    "sph_download_buffers": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_int64)] + [C.c_void_p] * 7),
     "sph_probe": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_double,
                               C.c_void_p]),
     "sph_output_write": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double]),

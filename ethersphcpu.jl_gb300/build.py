@@ -4,6 +4,7 @@ Compiles every translation unit of ``csrc/`` with nvcc in parallel and links
 ``lib/libethersph_gpu.so``.  Per-unit flags:
   sph_fp64.cu  -fmad=false            (plain FP64 path: no a*b+c contraction)
   sph_probe.cu -fmad=false            (FP64 interpolation, same rounding as the oracle)
+  sph_buffer.cu -fmad=false           (inlet/outlet moves and transfer decisions, as the oracle)
   sph_api.cu   -ffp-contract=off      (host constants round like the device code)
 """
 from __future__ import annotations
@@ -26,6 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relax
 UNIT_FLAGS = {
     "sph_fp64.cu": ["-fmad=false"],
     "sph_probe.cu": ["-fmad=false"],
+    "sph_buffer.cu": ["-fmad=false"],
     "sph_api.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 

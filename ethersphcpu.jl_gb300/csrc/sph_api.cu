@@ -64,6 +64,7 @@ int mode_of(int solve) {
     switch (solve) {
         case SPH_SOLVE_FLUID_WALL: return 0;
         case SPH_SOLVE_FLUID_VELOCITY_WALL: return 1;
+        case SPH_SOLVE_FLUID_INLET_OUTLET_WALL: return 3;
         default: return 2;
     }
 }
@@ -74,7 +75,10 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     std::memset(&S, 0, sizeof(S));
     if (p.dim != 2 && p.dim != 3) { err = "dim must be 2 or 3"; return false; }
     if (p.kernel < 0 || p.kernel > 3) { err = "unknown kernel"; return false; }
-    if (p.solve < 0 || p.solve > 3) { err = "unknown solve variant"; return false; }
+    if (p.solve < 0 || p.solve > 4) { err = "unknown solve variant"; return false; }
+    if (p.solve == SPH_SOLVE_FLUID_INLET_OUTLET_WALL && p.thermal) {
+        err = "the inlet/outlet solve has no thermal model"; return false;
+    }
     if (p.precision != SPH_PRECISION_FP64 && p.precision != SPH_PRECISION_FP32_COMPENSATED) {
         err = "unknown precision"; return false;
     }
@@ -216,6 +220,8 @@ struct SceneRec {
     std::vector<double> wx, wn, wv, wgap, wT, wkappa;  // host copy of the walls
     std::vector<int32_t> wkind;
     std::vector<int64_t> wgroup_end;  // end of each sph_upload_walls group in the host copy
+    double gap0 = 0.0;                // gap of the first uploaded fluid particle
+    bool uniform_fluid = true;        // every uploaded fluid particle has gap0
 };
 
 // First-fit allocator of ranges in [0, cap).
@@ -297,6 +303,21 @@ struct SphHandle {
     RangeAlloc cells, walls;
     // graph cache: key = (parity, pattern of Shepard steps) -> executable graph
     std::map<std::pair<int, std::vector<bool>>, cudaGraphExec_t> graphs;
+    // inlet/outlet buffers (sph_upload_buffers)
+    bool has_buffers = false;
+    bool buffers_started = false;  // br.first_step fixed by the first step after the upload
+    int64_t bcap = 0;
+    BufferState B[2]{};
+    BufferScratch bs{};
+    BufferRules br{};
+    int32_t* bn = nullptr;    // [2]: live buffer particles per parity
+    int64_t n_uploaded = 0;   // fluid particles of the last upload (ids 0 .. n-1)
+    std::vector<double> bgap_host;  // gaps of the uploaded buffer particles
+    bool buffer_gap_uniform(double g) const {
+        for (double v : bgap_host)
+            if (v != g) return false;
+        return true;
+    }
     sph::VtpWriter* out = nullptr;  // VTP output (sph_output_open)
     double* probe_buf = nullptr;    // device points + results of sph_probe
     int64_t probe_cap = 0;          // doubles in probe_buf
@@ -394,6 +415,20 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.tpp_continuity = h->tune[0];
     L.tpp_momentum = h->tune[1];
     L.tpp_reinit = h->tune[2];
+    if (h->has_buffers) {
+        // fluid particles made from the inlet are appended behind the live ones: the
+        // per-particle grids cover the capacity
+        L.cap = (int32_t)h->cap;
+        L.bf = h->B[h->par];
+        L.bf.n = h->bn + h->par;
+        L.bf.start = h->bs.start;
+        L.bf2 = h->B[h->par ^ 1];
+        L.bf2.n = h->bn + (h->par ^ 1);
+        L.bf2.start = h->bs.start;
+        L.bs = h->bs;
+        L.br = h->br;
+        L.bn_next = h->bn + (h->par ^ 1);
+    }
     return L;
 }
 
@@ -410,6 +445,7 @@ void enqueue_step(SphHandle* h, bool reinit) {
     launch_physics(0, L);
     launch_physics(1, L);
     if (reinit) launch_physics(2, L);
+    if (h->has_buffers) launch_buffers(L);  // before the scan advances the step counter
     launch_scan(L, 1);
     launch_place(L);
     h->par ^= 1;
@@ -429,6 +465,18 @@ int resort(SphHandle* h) {
     launch_place(L);
     SPH_CUDA(h, cudaGetLastError());
     h->par ^= 1;
+    if (h->has_buffers) {  // the buffers follow the fluid's buffer parity
+        const int from = h->par ^ 1, to = h->par;
+        const size_t n = (size_t)h->bcap, vb = vec_bytes(h->dim);
+        cudaStream_t st = h->stream;
+        SPH_CUDA(h, cudaMemcpyAsync(h->B[to].x, h->B[from].x, n * vb, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->B[to].v, h->B[from].v, n * vb, cudaMemcpyDeviceToDevice, st));
+        double* const src[5] = {h->B[from].rho, h->B[from].p, h->B[from].c, h->B[from].m, h->B[from].gap};
+        double* const dst[5] = {h->B[to].rho, h->B[to].p, h->B[to].c, h->B[to].m, h->B[to].gap};
+        for (int f = 0; f < 5; ++f) SPH_CUDA(h, cudaMemcpyAsync(dst[f], src[f], n * 8, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->B[to].order, h->B[from].order, n * 8, cudaMemcpyDeviceToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(h->bn + to, h->bn + from, 4, cudaMemcpyDeviceToDevice, st));
+    }
     SPH_CUDA(h, cudaStreamSynchronize(h->stream));
     return SPH_OK;
 }
@@ -852,6 +900,79 @@ int32_t open_scene(SphHandle* h, const SphParams& p, int64_t wall_cap, int64_t f
 
 }  // namespace
 
+namespace {
+
+// Device arrays of the buffers: both sorted sets, the sort scratch and the counters.
+int32_t allocate_buffers(SphHandle* h, int64_t cap) {
+    cudaError_t e;
+    const size_t n = (size_t)cap, ncell = (size_t)h->total_cells;
+    for (int b = 0; b < 2; ++b) {
+        BufferState& B = h->B[b];
+        double** d[5] = {&B.rho, &B.p, &B.c, &B.m, &B.gap};
+        if ((e = alloc_vec(h, (void**)&B.x, n)) != cudaSuccess) return cuda_fail(h, e, "buffer x");
+        if ((e = alloc_vec(h, (void**)&B.v, n)) != cudaSuccess) return cuda_fail(h, e, "buffer v");
+        for (double** f : d)
+            if ((e = dalloc(h, f, n)) != cudaSuccess) return cuda_fail(h, e, "buffer field");
+        if ((e = dalloc(h, &B.order, n)) != cudaSuccess) return cuda_fail(h, e, "buffer order");
+    }
+    BufferScratch& S = h->bs;
+    struct {
+        int32_t** p;
+        size_t n;
+    } ints[] = {{&S.key, n}, {&S.slot, n}, {&S.count, ncell}, {&S.start, ncell + 1},
+                {&S.block_sums, ncell / 4096 + 2}, {&S.pend, n}, {&S.npend, 1}, {&h->bn, 2}};
+    for (auto& a : ints)
+        if ((e = dalloc(h, a.p, a.n)) != cudaSuccess) return cuda_fail(h, e, "buffer scratch");
+    if ((e = dalloc(h, &S.tmp, n)) != cudaSuccess) return cuda_fail(h, e, "buffer scratch");
+    S.cap = (int32_t)cap;
+    h->bcap = cap;
+    return SPH_OK;
+}
+
+// The live buffer particles of the current parity, on the host (sorted order).
+struct HostBuffers {
+    int32_t n = 0;
+    std::vector<char> x, v;
+    std::vector<double> rho, p, c, m, gap;
+    std::vector<int64_t> order;
+};
+
+int32_t read_buffers(SphHandle* h, HostBuffers& H) {
+    cudaStream_t st = h->stream;
+    SPH_CUDA(h, cudaMemcpyAsync(&H.n, h->bn + h->par, 4, cudaMemcpyDeviceToHost, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    if (H.n < 0 || H.n > h->bcap) return fail(h, SPH_ERR_STATE, "buffer count out of range");
+    const size_t n = (size_t)H.n, vb = vec_bytes(h->dim);
+    const BufferState& B = h->B[h->par];
+    H.x.resize(n * vb);
+    H.v.resize(n * vb);
+    H.order.resize(n);
+    std::vector<double>* f[5] = {&H.rho, &H.p, &H.c, &H.m, &H.gap};
+    const double* src[5] = {B.rho, B.p, B.c, B.m, B.gap};
+    if (n > 0) {
+        SPH_CUDA(h, cudaMemcpyAsync(H.x.data(), B.x, n * vb, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(h, cudaMemcpyAsync(H.v.data(), B.v, n * vb, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(h, cudaMemcpyAsync(H.order.data(), B.order, n * 8, cudaMemcpyDeviceToHost, st));
+        for (int k = 0; k < 5; ++k) {
+            f[k]->resize(n);
+            SPH_CUDA(h, cudaMemcpyAsync(f[k]->data(), src[k], n * 8, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    return SPH_OK;
+}
+
+// Sorted positions of the inlet (which = 0) or outlet (1) particles, in ascending order.
+std::vector<int64_t> buffer_rank(const HostBuffers& H, int which) {
+    std::vector<int64_t> sel;
+    for (int64_t b = 0; b < H.n; ++b)
+        if (((H.order[b] & kOutletBit) != 0) == (which == 1)) sel.push_back(b);
+    std::sort(sel.begin(), sel.end(), [&](int64_t a, int64_t b) { return H.order[a] < H.order[b]; });
+    return sel;
+}
+
+}  // namespace
+
 extern "C" {
 
 int32_t sph_version(void) { return SPH_ABI_VERSION; }
@@ -898,12 +1019,20 @@ int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double*
     SceneRec& R = h->scenes[0];
     bool uniform = true;
     for (int64_t i = 1; i < n; ++i) uniform &= gap[i] == gap[0];
-    R.dev.uniform_gap = uniform ? 1 : 0;
+    R.gap0 = n > 0 ? gap[0] : 0.0;
+    R.uniform_fluid = uniform;
+    R.dev.uniform_gap = uniform && (!h->has_buffers || h->buffer_gap_uniform(R.gap0)) ? 1 : 0;
     int32_t rc = upload_scene_const(h, 0);
     if (rc != SPH_OK) return rc;
     rc = append_fluid(h, 0, 0, n, x, v, rho, p, c, mass, gap, t, kappa, cp);  // replaces the state
     if (rc != SPH_OK) return rc;
     h->have_fluid = true;
+    h->n_uploaded = n;
+    if (h->has_buffers) {  // fluid made from the inlet continues the ids of this upload
+        h->br.id_base = n;
+        for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+        h->graphs.clear();
+    }
     return SPH_OK;
 }
 
@@ -925,6 +1054,17 @@ int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_step before sph_upload_fluid");
     if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
     if (nsteps == 0) return SPH_OK;
+    if (h->has_buffers) {
+        if (!h->buffers_started) {  // ids of inlet copies count steps from here
+            h->br.first_step = first_step;
+            h->buffers_started = true;
+            for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+            h->graphs.clear();
+        }
+        if (first_step < h->br.first_step) return fail(h, SPH_ERR_ARG, "steps before the buffer upload");
+        if (h->br.id_base + (first_step + nsteps - h->br.first_step) * h->br.n_inlet > INT32_MAX)
+            return fail(h, SPH_ERR_ARG, "fluid ids of inlet copies would pass 2^31 - 1");
+    }
     if (first_step != h->scenes[0].step_host) {  // the device counter only needs a reset on a jump
         int32_t rc = set_scene_step(h, 0, first_step);
         if (rc != SPH_OK) return rc;
@@ -944,6 +1084,8 @@ int32_t sph_synchronize(SphHandle* h) {
     for (const SceneRec& R : h->scenes) nan_check |= R.used && R.dev.nan_check;
     if ((status & kStatusNonFinite) && nan_check)
         return fail(h, SPH_ERR_NAN, "non-finite fluid state (density, velocity or position)");
+    if (status & kStatusBufferOverflow)
+        return fail(h, SPH_ERR_GRID_OVERFLOW, "inlet/outlet transfers exceeded the fluid or buffer capacity");
     return SPH_OK;
 }
 
@@ -1205,6 +1347,7 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
     Lh.nx.rho = L.st.rho;
     Lh.nx.T = L.st.T;
     L.force_reinit = 1;
+    L.bs.npend = nullptr;  // timed momentum launches mark no particle for the outlet
     const int par = h->par;
     auto run = [&](int stage) {
         switch (stage) {
@@ -1270,6 +1413,7 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
                 for (int block : blocks) {
                     LaunchCtx L = make_ctx(h);
                     L.force_reinit = 1;
+                    L.bs.npend = nullptr;  // trial launches mark no particle for the outlet
                     L.block = block;
                     L.tpp_continuity = L.tpp_momentum = L.tpp_reinit = tpp;
                     launch_physics(stage, L);  // warm-up
@@ -1294,6 +1438,7 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         // restore what the timed launches touched: p and c, and the arrivals left in
         // count[]; every other field they wrote is rebuilt by the next step before use
         SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
+        if (h->has_buffers) SPH_CUDA(h, cudaMemsetAsync(h->bs.npend, 0, 4, st));  // outlet marks of the trials
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par].p, h->S[par ^ 1].p, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par].c, h->S[par ^ 1].c, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaGetLastError());
@@ -1393,6 +1538,162 @@ int32_t sph_output_flush(SphHandle* h) {
     std::string err;
     int rc = h->out->flush(err);
     if (rc != SPH_OK) return fail(h, rc, err);
+    return SPH_OK;
+}
+
+int32_t sph_upload_buffers(SphHandle* h, const SphBufferRules* rules, int64_t capacity, int64_t n_inlet,
+                           const double* x, const double* v, const double* rho, const double* p, const double* c,
+                           const double* mass, const double* gap, int64_t n_outlet, const double* ox,
+                           const double* ov, const double* orho, const double* op, const double* oc,
+                           const double* omass, const double* ogap) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "inlet/outlet buffers are for single-scene handles");
+    if (h->mode != 3) return fail(h, SPH_ERR_STATE, "buffers need solve = SPH_SOLVE_FLUID_INLET_OUTLET_WALL");
+    if (!rules || n_inlet < 0 || n_outlet < 0 || capacity < n_inlet + n_outlet || capacity < 1 ||
+        capacity > INT32_MAX / 2)
+        return fail(h, SPH_ERR_ARG, "sph_upload_buffers: invalid counts or capacity");
+    if ((n_inlet > 0 && (!x || !v || !rho || !p || !c || !mass || !gap)) ||
+        (n_outlet > 0 && (!ox || !ov || !orho || !op || !oc || !omass || !ogap)))
+        return fail(h, SPH_ERR_ARG, "sph_upload_buffers: missing arrays");
+    const int dim = h->dim;
+    if (capacity > h->bcap) {
+        int32_t rc = allocate_buffers(h, capacity);
+        if (rc != SPH_OK) return rc;
+    }
+    // rules
+    BufferRules br{};
+    for (int k = 0; k < 3; ++k) {
+        br.in_n[k] = rules->inlet_normal[k];
+        br.in_shift[k] = rules->inlet_shift[k];
+        br.out_n[k] = rules->outlet_normal[k];
+        br.drop_n[k] = rules->drop_normal[k];
+    }
+    br.in_d = rules->inlet_offset;
+    br.out_d = rules->outlet_offset;
+    br.drop_d = rules->drop_offset;
+    br.n_inlet = n_inlet;
+    br.id_base = h->n_uploaded;
+    br.first_step = h->scenes[0].step_host;
+    // host sort by (cell, order)
+    const SceneRec& R = h->scenes[0];
+    const int64_t n = n_inlet + n_outlet;
+    std::vector<int64_t> order(n);
+    std::vector<int32_t> key(n);
+    auto xs = [&](int64_t b, int k) { return b < n_inlet ? x[b * dim + k] : ox[(b - n_inlet) * dim + k]; };
+    for (int64_t b = 0; b < n; ++b) {
+        order[b] = b < n_inlet ? b : (kOutletBit | (b - n_inlet));
+        double xb[3] = {0, 0, 0};
+        for (int k = 0; k < dim; ++k) xb[k] = xs(b, k);
+        key[b] = host_cell_key(R.dev, dim, xb);
+    }
+    std::vector<int64_t> idx(n);
+    for (int64_t b = 0; b < n; ++b) idx[b] = b;
+    std::sort(idx.begin(), idx.end(), [&](int64_t a, int64_t b) {
+        return key[a] != key[b] ? key[a] < key[b] : order[a] < order[b];
+    });
+    std::vector<int32_t> start((size_t)h->total_cells + 1, 0);
+    for (int64_t b = 0; b < n; ++b) start[key[b] + 1]++;
+    for (size_t q = 0; q + 1 < start.size(); ++q) start[q + 1] += start[q];
+    const size_t vb = vec_bytes(dim);
+    std::vector<char> hx(n * vb, 0), hv(n * vb, 0);
+    std::vector<double> hf[5];
+    for (auto& f : hf) f.resize(n);
+    std::vector<int64_t> ho(n);
+    h->bgap_host.assign(n, 0.0);
+    for (int64_t q = 0; q < n; ++q) {
+        const int64_t b = idx[q];
+        const bool in = b < n_inlet;
+        const int64_t j = in ? b : b - n_inlet;
+        for (int k = 0; k < dim; ++k) {
+            ((double*)(hx.data() + q * vb))[k] = in ? x[j * dim + k] : ox[j * dim + k];
+            ((double*)(hv.data() + q * vb))[k] = in ? v[j * dim + k] : ov[j * dim + k];
+        }
+        hf[0][q] = in ? rho[j] : orho[j];
+        hf[1][q] = in ? p[j] : op[j];
+        hf[2][q] = in ? c[j] : oc[j];
+        hf[3][q] = in ? mass[j] : omass[j];
+        hf[4][q] = in ? gap[j] : ogap[j];
+        h->bgap_host[q] = hf[4][q];
+        ho[q] = order[b];
+    }
+    cudaStream_t st = h->stream;
+    const BufferState& B = h->B[h->par];
+    double* dst[5] = {B.rho, B.p, B.c, B.m, B.gap};
+    if (n > 0) {
+        SPH_CUDA(h, cudaMemcpyAsync(B.x, hx.data(), n * vb, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(B.v, hv.data(), n * vb, cudaMemcpyHostToDevice, st));
+        for (int f = 0; f < 5; ++f)
+            SPH_CUDA(h, cudaMemcpyAsync(dst[f], hf[f].data(), n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(B.order, ho.data(), n * 8, cudaMemcpyHostToDevice, st));
+    }
+    SPH_CUDA(h, cudaMemcpyAsync(h->bs.start, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st));
+    const int32_t counts[2] = {(int32_t)n, (int32_t)n};
+    SPH_CUDA(h, cudaMemcpyAsync(h->bn, counts, 8, cudaMemcpyHostToDevice, st));
+    SPH_CUDA(h, cudaMemsetAsync(h->bs.count, 0, sizeof(int32_t) * (size_t)h->total_cells, st));
+    SPH_CUDA(h, cudaMemsetAsync(h->bs.npend, 0, 4, st));
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    h->br = br;
+    h->has_buffers = true;
+    h->buffers_started = false;
+    // fluid made from the inlet (or a buffer with another gap) breaks the uniform-gap shortcut
+    SceneRec& Rw = h->scenes[0];
+    const bool uniform = Rw.uniform_fluid && h->buffer_gap_uniform(Rw.gap0);
+    if ((Rw.dev.uniform_gap != 0) != uniform) {
+        Rw.dev.uniform_gap = uniform ? 1 : 0;
+        int32_t rc = upload_scene_const(h, 0);
+        if (rc != SPH_OK) return rc;
+    }
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    return SPH_OK;
+}
+
+int32_t sph_set_buffer_velocity(SphHandle* h, int32_t which, int64_t n, const double* v) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->has_buffers) return fail(h, SPH_ERR_STATE, "no inlet/outlet buffers");
+    if ((which != 0 && which != 1) || n < 0 || (n > 0 && !v)) return fail(h, SPH_ERR_ARG, "bad arguments");
+    HostBuffers H;
+    int32_t rc = read_buffers(h, H);
+    if (rc != SPH_OK) return rc;
+    const std::vector<int64_t> sel = buffer_rank(H, which);
+    if ((int64_t)sel.size() != n) return fail(h, SPH_ERR_ARG, "velocity count differs from the particle count");
+    const int dim = h->dim;
+    const size_t vb = vec_bytes(dim);
+    for (int64_t q = 0; q < n; ++q)
+        for (int k = 0; k < dim; ++k) ((double*)(H.v.data() + sel[q] * vb))[k] = v[q * dim + k];
+    if (H.n > 0) {
+        SPH_CUDA(h, cudaMemcpyAsync(h->B[h->par].v, H.v.data(), (size_t)H.n * vb, cudaMemcpyHostToDevice,
+                                    h->stream));
+        SPH_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
+    return SPH_OK;
+}
+
+int32_t sph_download_buffers(SphHandle* h, int32_t which, int64_t capacity, int64_t* n_out, double* x, double* v,
+                             double* rho, double* p, double* c, double* mass, double* gap) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    if (!h->has_buffers) return fail(h, SPH_ERR_STATE, "no inlet/outlet buffers");
+    if ((which != 0 && which != 1) || !n_out) return fail(h, SPH_ERR_ARG, "bad arguments");
+    HostBuffers H;
+    int32_t rc = read_buffers(h, H);
+    if (rc != SPH_OK) return rc;
+    const std::vector<int64_t> sel = buffer_rank(H, which);
+    *n_out = (int64_t)sel.size();
+    if ((int64_t)sel.size() > capacity) return fail(h, SPH_ERR_ARG, "caller arrays too small for the buffers");
+    const int dim = h->dim;
+    const size_t vb = vec_bytes(dim);
+    for (size_t q = 0; q < sel.size(); ++q) {
+        const int64_t b = sel[q];
+        for (int k = 0; k < dim; ++k) {
+            if (x) x[q * dim + k] = ((const double*)(H.x.data() + b * vb))[k];
+            if (v) v[q * dim + k] = ((const double*)(H.v.data() + b * vb))[k];
+        }
+        if (rho) rho[q] = H.rho[b];
+        if (p) p[q] = H.p[b];
+        if (c) c[q] = H.c[b];
+        if (mass) mass[q] = H.m[b];
+        if (gap) gap[q] = H.gap[b];
+    }
     return SPH_OK;
 }
 

@@ -22,7 +22,7 @@ namespace sph {
 constexpr int32_t kDeadKey = 0x7fffffff;
 
 // Status bits written by kernels (atomicOr) and read by the host after a step.
-enum : int32_t { kStatusNonFinite = 1, kStatusClamped = 2 };
+enum : int32_t { kStatusNonFinite = 1, kStatusClamped = 2, kStatusBufferOverflow = 4 };
 
 // Per-scene constants.  Every derived constant is formed on the host with the same
 // IEEE operation sequence the Julia code would use at the point of use, so using the
@@ -148,6 +148,63 @@ struct SortScratch {
     int32_t* status;    // device scalar: status bits
     int64_t* scene_step;  // per scene: number of the step being run
 };
+
+// ---------------------------------------------------------------- inlet/outlet buffers
+// Buffer particles (FluidInletOutletWallSolve.jl:8-262): fluid particles of the inlet and
+// outlet regions.  They are neighbours of the fluid in continuity and momentum but are
+// not updated by them: they move with their own velocity (x += v dt) and keep their
+// density, pressure and sound speed.  Sorted by (cell, order) like the fluid by (cell, id).
+// order: bit 62 = outlet; inlet particle k: k; outlet particle uploaded as k:
+// kOutletBit | k; fluid particle id moved to the outlet at step first_step + r:
+// kOutletBit | (r + 1) << 32 | id.  Ascending order is the reference's vector order.
+constexpr int64_t kOutletBit = int64_t(1) << 62;
+
+struct BufferState {
+    void* x;  // V
+    void* v;  // V
+    double* rho;
+    double* p;
+    double* c;
+    double* m;
+    double* gap;
+    int64_t* order;
+    const int32_t* start;  // cell starts of the buffer particles (scene grid, ncells + 1)
+    const int32_t* n;      // device scalar: live buffer particles; null when the handle has none
+};
+
+struct BufferScratch {
+    int32_t* key;
+    int32_t* slot;
+    int32_t* count;    // per cell
+    int32_t* start;    // per cell + 1 (the next step's BufferState::start)
+    int64_t* tmp;      // order by arrival slot
+    int32_t* block_sums;
+    int32_t* pend;     // fluid particles moving to the outlet this step
+    int32_t* npend;    // device scalar
+    int32_t cap;       // buffer capacity (also the capacity of pend)
+};
+
+// Transfer rules: plane tests n.x > d (the example's checks compare one coordinate with a
+// bound, PoiseuilleFlow2D.jl:146-151), the inlet shift of the modify step, and the id
+// arithmetic of fluid particles created from the inlet.
+struct BufferRules {
+    double in_n[3], in_d, in_shift[3];  // inlet_into_calculation_domain_check / _modify
+    double out_n[3], out_d;             // outlet_out_calculation_domain_check
+    double drop_n[3], drop_d;           // outlet_out_check
+    int64_t n_inlet;                    // inlet particles (their count never changes)
+    int64_t id_base;                    // id of the first fluid particle made from the inlet
+    int64_t first_step;                 // step of the buffer upload
+};
+
+// n.x > d, products and sums rounded one by one, x ascending (no contraction, so every
+// form and the CPU restatement take the same decisions).
+template <int DIM>
+__device__ __forceinline__ bool beyond_plane(const double n[3], double d, const double x[DIM]) {
+    double s = __dmul_rn(n[0], x[0]);
+    s = __dadd_rn(s, __dmul_rn(n[1], x[1]));
+    if (DIM == 3) s = __dadd_rn(s, __dmul_rn(n[2], x[DIM - 1]));
+    return s > d;
+}
 
 // ---------------------------------------------------------------- grid
 __device__ __forceinline__ int32_t cell_coord(double x, const SceneDev& S, int a) {

@@ -29,7 +29,7 @@ namespace sph {
 
 namespace {
 
-enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2 };
+enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2, kModeBuffers = 3 };
 
 struct Kahan {
     float s = 0.f, c = 0.f;
@@ -234,7 +234,8 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 
 // -------------------------------------------------------------------- K4 (FP32)
 template <int DIM, int KK, int TPP, bool PF>
-__global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap) {
+__global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
+                                 BufferState bf) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *sc.n_live) return;
@@ -283,8 +284,12 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         }
         drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
     });
-    const double dr = group_sum<TPP>(drho.value(), group_mask<TPP>());
+    double dr = group_sum<TPP>(drho.value(), group_mask<TPP>());
     if (lane != 0) return;
+    if (bf.n) {  // inlet/outlet buffer neighbours, FP64
+        using V = typename VecT<DIM>::T;
+        dr += buffer_drho<DIM, KK>(S, bf, c, ((const V*)st.x)[i], ((const V*)st.v)[i]);
+    }
     double rho = st.rho[i];
     rho += dr * S.dt;
     const double rr = rho / S.rho0;
@@ -315,7 +320,7 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
 // prefetched candidate would spill) and is therefore limited to blocks of 256 threads.
 template <int DIM, int KK, int MODE, int TPP, bool PF>
 __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
-                               SortScratch sc, int32_t cap) {
+                               SortScratch sc, int32_t cap, BufferState bf, BufferScratch bs, BufferRules br) {
     using V = typename VecT<DIM>::T;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
@@ -470,7 +475,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
                     acc[2] += wf * n[2];
                 }
             }
-            if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
+            if (MODE == kModeWallPressure || MODE == kModeThermal) {  // PressureForce.jl:29-33
                 float prho2 = P_i + S.P_bg_f;
                 prho2 += fabsf(prho2) * 0.01f * W * inv_Wg_i;
                 const float gp = -m_i * prho2 * dW * inv_r;
@@ -509,6 +514,10 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     const int64_t step = sc.scene_step[s];
     const V x0 = ((const V*)st.x)[i];
     const V v0 = ((const V*)st.v)[i];
+    if (MODE == kModeBuffers && bf.n) {  // inlet/outlet buffer neighbours, FP64
+        const double rho_d = st.rhoc[i], gap_d = st.gap[i];
+        buffer_dv<DIM, KK>(S, bf, c, x0, v0, rho_d, st.P[i], gap_d, kernel_w<KK>(gap_d, S), S.nu0 * rho_d, dvd);
+    }
     const double dt = S.dt;
     double body[DIM];
     if (MODE == kModeThermal) {
@@ -561,6 +570,12 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     }
     if (dead) {
         sc.key[i] = kDeadKey;
+    } else if (MODE == kModeBuffers && bs.npend && beyond_plane<DIM>(br.out_n, br.out_d, xn)) {
+        // outlet_out_calculation_domain_check: leaves the fluid, joins the outlet
+        sc.key[i] = kDeadKey;
+        const int32_t k = atomicAdd(bs.npend, 1);
+        if (k < bs.cap) bs.pend[k] = i;
+        else atomicOr(sc.status, kStatusBufferOverflow);
     } else {
         const int32_t key = cell_key<DIM>(xo, S);
         sc.key[i] = key;
@@ -612,19 +627,22 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        k_continuity_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
+        k_continuity_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap, L.bf);
     } else if (stage == 2) {
         k_reinit_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap,
                                                                       L.force_reinit);
     } else if (mode == kModeFluidWall) {
-        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
-                                                                                       L.sc, L.cap);
+        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
     } else if (mode == kModeWallPressure) {
-        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx,
-                                                                                          L.wl, L.sc, L.cap);
+        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
+    } else if (mode == kModeBuffers) {
+        k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
     } else {
-        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl,
-                                                                                     L.sc, L.cap);
+        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
     }
 }
 

@@ -21,11 +21,11 @@
 namespace sph {
 
 // Solve variants: which wall terms and which body force.
-enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2 };
+enum { kModeFluidWall = 0, kModeWallPressure = 1, kModeThermal = 2, kModeBuffers = 3 };
 
 template <int DIM, int KK>
 __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restrict__ scenes, SortedState st,
-                                                         SortScratch sc, int32_t cap) {
+                                                         SortScratch sc, int32_t cap, BufferState bf) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
@@ -61,6 +61,29 @@ __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restr
             drho += dotd<DIM>(vv, g) * st.m[j];
         }
     });
+    if (bf.n) {  // inlet/outlet buffer neighbours (FluidInletOutletWallSolve.jl:59-72)
+        const V* __restrict__ bx = (const V*)bf.x;
+        const V* __restrict__ bv = (const V*)bf.v;
+        walk_cells<DIM>(S, bf.start, c, [&](int jb, int je) {
+            for (int b = jb; b < je; ++b) {
+                double rv[DIM];
+                make_rvec<DIM>(xi, bx[b], S, rv);
+                const double d2 = norm_sq<DIM>(rv);
+                if (!(d2 <= S.rc2)) continue;
+                const double r = sqrt(d2);
+                double W, dW;
+                kernel_wdw<KK>(r, S, W, dW);
+                double g[DIM];
+                grad_vec<DIM>(dW, r, rv, g);
+                const V vb = bv[b];
+                double vv[DIM];
+                vv[0] = vi.x - vb.x;
+                vv[1] = vi.y - vb.y;
+                if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vb, DIM - 1);
+                drho += dotd<DIM>(vv, g) * bf.m[b];
+            }
+        });
+    }
     double rho = st.rho[i];
     rho += drho * S.dt;  // written to rhoc, so the kernel can be re-run on the same input
     const double rr = rho / S.rho0;
@@ -75,7 +98,8 @@ __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restr
 template <int DIM, int KK, int MODE>
 __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restrict__ scenes, SortedState st,
                                                        NextState nx, WallState wl, SortScratch sc,
-                                                       int32_t cap) {
+                                                       int32_t cap, BufferState bf, BufferScratch bs,
+                                                       BufferRules br) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
@@ -153,6 +177,44 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
         }
     });
 
+    // ---- inlet/outlet buffer neighbours: pressureForce! + viscosityForce! with the
+    // buffer particle's frozen density and pressure (FluidInletOutletWallSolve.jl:125-158)
+    if (MODE == kModeBuffers && bf.n) {
+        const V* __restrict__ bx = (const V*)bf.x;
+        const V* __restrict__ bv = (const V*)bf.v;
+        walk_cells<DIM>(S, bf.start, c, [&](int jb, int je) {
+            for (int b = jb; b < je; ++b) {
+                double rv[DIM];
+                make_rvec<DIM>(xi, bx[b], S, rv);
+                const double d2 = norm_sq<DIM>(rv);
+                if (!(d2 <= S.rc2)) continue;
+                const double r = sqrt(d2);
+                double W, dW;
+                kernel_wdw<KK>(r, S, W, dW);
+                double g[DIM];
+                grad_vec<DIM>(dW, r, rv, g);
+                const V vb = bv[b];
+                double vv[DIM];
+                vv[0] = vi.x - vb.x;
+                vv[1] = vi.y - vb.y;
+                if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vb, DIM - 1);
+                const double rho_b = bf.rho[b];
+                const double m_b = bf.m[b];
+                const double gap_b = bf.gap[b];
+                double prho2 = P_i + bf.p[b] / (rho_b * rho_b);
+                const double Wg = gap_b == gap_i ? Wg_i : kernel_w<KK>((gap_i + gap_b) / 2.0, S);
+                prho2 += fabs(prho2) * 0.01 * W / Wg;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) dv[k] += -m_b * prho2 * g[k];
+                const double sum_rho = rho_i + rho_b;
+                const double mu_b = S.nu0 * rho_b;
+                const double f = 4.0 * (mu_i + mu_b) * r * dW / (sum_rho * sum_rho) / (r * r + S.hh001);
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) dv[k] += m_b * f * vv[k];
+            }
+        });
+    }
+
     // ---- walls: wallForce! (+ background pressureForce!) + viscosityForce! (+ heat)
     if (wl.n > 0) {
         const V* __restrict__ wx = (const V*)wl.x;
@@ -201,7 +263,7 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
                         for (int k = 0; k < DIM; ++k) dv[k] += wf * n[k];
                     }
                 }
-                if (MODE != kModeFluidWall) {  // PressureForce.jl:29-33
+                if (MODE == kModeWallPressure || MODE == kModeThermal) {  // PressureForce.jl:29-33
                     double prho2 = P_i + S.P_bg;
                     prho2 += fabs(prho2) * 0.01 * W / Wgap_bg;
 #pragma unroll
@@ -282,6 +344,12 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
     }
     if (dead) {
         sc.key[i] = kDeadKey;
+    } else if (MODE == kModeBuffers && bs.npend && beyond_plane<DIM>(br.out_n, br.out_d, xn)) {
+        // outlet_out_calculation_domain_check: leaves the fluid, joins the outlet
+        sc.key[i] = kDeadKey;
+        const int32_t k = atomicAdd(bs.npend, 1);
+        if (k < bs.cap) bs.pend[k] = i;
+        else atomicOr(sc.status, kStatusBufferOverflow);
     } else {
         const int32_t key = cell_key<DIM>(xo, S);
         sc.key[i] = key;
@@ -328,12 +396,13 @@ namespace {
 template <int DIM, int KK>
 void launch_k4(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
-    k_continuity_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap);
+    k_continuity_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap, L.bf);
 }
 template <int DIM, int KK, int MODE>
 void launch_k5(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
-    k_momentum_fp64<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap);
+    k_momentum_fp64<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs,
+                                                                 L.br);
 }
 template <int DIM, int KK>
 void launch_k6(const LaunchCtx& L) {
@@ -349,6 +418,7 @@ void dispatch_kk(int kk, int stage, int mode, const LaunchCtx& L) {
         else if (stage == 2) launch_k6<DIM, KKV>(L);                            \
         else if (mode == kModeFluidWall) launch_k5<DIM, KKV, kModeFluidWall>(L); \
         else if (mode == kModeWallPressure) launch_k5<DIM, KKV, kModeWallPressure>(L); \
+        else if (mode == kModeBuffers) launch_k5<DIM, KKV, kModeBuffers>(L);    \
         else launch_k5<DIM, KKV, kModeThermal>(L);                              \
         break;
     switch (kk) {

@@ -28,6 +28,11 @@ struct LaunchCtx {
     // launch shape of the FP32 gathers (lanes per particle, threads per block)
     int block;
     int tpp_continuity, tpp_momentum, tpp_reinit;
+    // inlet/outlet buffers (bf.n == nullptr: none): current and next sorted buffers
+    BufferState bf, bf2;
+    BufferScratch bs;
+    BufferRules br;
+    int32_t* bn_next;  // live buffer particles after the buffer sort being built
 };
 
 // stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init
@@ -35,6 +40,11 @@ void launch_physics_fp64(int stage, const LaunchCtx& L);
 void launch_physics_fp32(int stage, const LaunchCtx& L);
 void launch_physics_fp32_2d(int stage, const LaunchCtx& L);
 void launch_physics_fp32_3d(int stage, const LaunchCtx& L);
+
+// Buffer particles after the gathers of a step (K4-K6): move them, copy inlet particles
+// that crossed into the fluid, move the fluid particles K5 marked to the outlet, drop
+// outlet particles, and sort the buffers by (cell, order) into L.bf2.
+void launch_buffers(const LaunchCtx& L);
 
 // Cell hash of the unsorted positions in L.nx.x (used once after an upload).
 void launch_hash(const LaunchCtx& L);

@@ -235,4 +235,74 @@ __device__ __forceinline__ void carry_frozen(int i, const SceneDev& S, const Sor
     sc.slot[i] = atomicAdd(sc.count + key, 1);
 }
 
+// ---------------------------------------------------------------- buffer neighbours
+// Sums of a fluid particle over the inlet/outlet buffer particles within r_cut, in FP64
+// (FluidInletOutletWallSolve.jl:59-72 continuity, :125-158 pressure and viscosity): the
+// FP32 form adds them to its compensated sums after the lane reduction.
+template <int DIM, int KK, typename V>
+__device__ __forceinline__ double buffer_drho(const SceneDev& S, const BufferState& bf, const int32_t c[3],
+                                              const V& xi, const V& vi) {
+    const V* __restrict__ bx = (const V*)bf.x;
+    const V* __restrict__ bv = (const V*)bf.v;
+    double drho = 0.0;
+    walk_cells<DIM>(S, bf.start, c, [&](int jb, int je) {
+        for (int b = jb; b < je; ++b) {
+            double rv[DIM];
+            make_rvec<DIM>(xi, bx[b], S, rv);
+            const double d2 = norm_sq<DIM>(rv);
+            if (!(d2 <= S.rc2)) continue;
+            const double r = sqrt(d2);
+            double W, dW;
+            kernel_wdw<KK>(r, S, W, dW);
+            double g[DIM];
+            grad_vec<DIM>(dW, r, rv, g);
+            const V vb = bv[b];
+            double vv[DIM];
+            vv[0] = vi.x - vb.x;
+            vv[1] = vi.y - vb.y;
+            if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vb, DIM - 1);
+            drho += dotd<DIM>(vv, g) * bf.m[b];
+        }
+    });
+    return drho;
+}
+
+template <int DIM, int KK, typename V>
+__device__ __forceinline__ void buffer_dv(const SceneDev& S, const BufferState& bf, const int32_t c[3], const V& xi,
+                                          const V& vi, double rho_i, double P_i, double gap_i, double Wg_i,
+                                          double mu_i, double dv[DIM]) {
+    const V* __restrict__ bx = (const V*)bf.x;
+    const V* __restrict__ bv = (const V*)bf.v;
+    walk_cells<DIM>(S, bf.start, c, [&](int jb, int je) {
+        for (int b = jb; b < je; ++b) {
+            double rv[DIM];
+            make_rvec<DIM>(xi, bx[b], S, rv);
+            const double d2 = norm_sq<DIM>(rv);
+            if (!(d2 <= S.rc2)) continue;
+            const double r = sqrt(d2);
+            double W, dW;
+            kernel_wdw<KK>(r, S, W, dW);
+            double g[DIM];
+            grad_vec<DIM>(dW, r, rv, g);
+            const V vb = bv[b];
+            double vv[DIM];
+            vv[0] = vi.x - vb.x;
+            vv[1] = vi.y - vb.y;
+            if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vb, DIM - 1);
+            const double rho_b = bf.rho[b];
+            const double m_b = bf.m[b];
+            const double gap_b = bf.gap[b];
+            double prho2 = P_i + bf.p[b] / (rho_b * rho_b);
+            const double Wg = gap_b == gap_i ? Wg_i : kernel_w<KK>((gap_i + gap_b) / 2.0, S);
+            prho2 += fabs(prho2) * 0.01 * W / Wg;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) dv[k] += -m_b * prho2 * g[k];
+            const double sum_rho = rho_i + rho_b;
+            const double f = 4.0 * (mu_i + S.nu0 * rho_b) * r * dW / (sum_rho * sum_rho) / (r * r + S.hh001);
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) dv[k] += m_b * f * vv[k];
+        }
+    });
+}
+
 }  // namespace sph

@@ -272,6 +272,63 @@ def poiseuille_periodic_2d(H=1e-3, length_factor=4.0, nu=1e-6, reynolds=0.5, n_a
                  periodic_x=True, meta=dict(H=H, nu=nu, f=f, umax=umax, dx=dx, L=L))
 
 
+def poiseuille_inlet_outlet_2d(H=1e-2, length_factor=4.0, nu=1e-6, f=8e-5, n_across=20, total_step=2000,
+                               reinit=5, kernel="WendlandC2", rho0=1000.0, start="steady",
+                               name="poiseuille_inlet_outlet_2d"):
+    """The reference's channel flow with inlet and outlet buffers (PoiseuilleFlow2D.jl):
+    channel H x 4H, 3 layers of inlet particles upstream of x = 0 and of outlet particles
+    downstream of x = 4H, 3 wall layers below and above reaching 6 layers past both ends,
+    WendlandC2 with r_cut = 3 dx, body force f, U_max = f H^2 / (8 nu), c0 = 10 U_max,
+    p0 = 0.02 rho0 c0^2, gamma = 7, dt = 0.1 r_cut / c0.  The example starts from the
+    transient profile at t = 0 (at rest) and lets a host callback set the buffers to the
+    analytic profile every step; start="steady" starts every particle on the steady
+    profile instead, so that particles cross the inlet and outlet from the first steps.
+    meta holds the inlet and outlet particles and the InletOutletRules."""
+    from .types import InletOutletRules
+    dim = 2
+    dx = H / n_across
+    rc = 3.0 * dx
+    kernel = SmoothKernel(rc, dim, kernel)
+    umax = f / 2.0 / nu / 4.0 * H * H
+    c0 = 10.0 * umax
+    p0 = 0.02 * rho0 * c0 * c0
+    model = CommonWeaklyCompressibleLiquidModel(rho0, c0, p0, 7, nu * rho0, np.array([f, 0.0]))
+    dt = min(0.1 * rc / c0, 0.1 * kernel.h_ * kernel.h_ / nu)
+    td = DensityReinitializedFixedTimeIntervalForwardEuler(dt, total_step, 100, reinit, reinit)
+    L = length_factor * H
+    nxl = int(round(L / dx))
+    t = 3
+
+    def block(x0, ncol):
+        g = CommonLiquidParticles(ncol * n_across, dim)
+        g.x_vec_[:] = lattice_2d(x0, 0.0, ncol, n_across, dx)
+        g.rho_[:] = rho0
+        g.p_[:] = p0
+        g.c_[:] = c0
+        g.mass_[:] = rho0 * dx * dx
+        g.gap_[:] = dx
+        y = g.x_vec_[:, 1]
+        g.v_vec_[:, 0] = (f / 2.0 / nu * y * (H - y) if start == "steady"
+                          else poiseuille_ux_theory(y, 0.0, H, nu, f))
+        return g
+
+    fluid = block(0.0, nxl)
+    inlet = block(-t * dx, t)
+    outlet = block(L, t)
+    W = CompulsiveWallParticles
+    more = 3
+    wcols = nxl + 2 * (t + more)
+    walls = W.vcat(_walls(W, lattice_2d(-(t + more) * dx, -t * dx, wcols, t, dx), [0.0, 1.0], dx),
+                   _walls(W, lattice_2d(-(t + more) * dx, H, wcols, t, dx), [0.0, -1.0], dx))
+    lo = (-(t + more) * dx - rc, -t * dx - rc)
+    hi = (L + (t + more) * dx + rc, H + t * dx + rc)
+    rules = InletOutletRules(inlet_normal=(1.0, 0.0), inlet_offset=0.0, inlet_shift=(-t * dx, 0.0),
+                             outlet_normal=(1.0, 0.0), outlet_offset=L,
+                             drop_normal=(1.0, 0.0), drop_offset=L + t * dx)
+    return Scene(name, fluid, [walls], kernel, model, td, _abi.SOLVE_FLUID_INLET_OUTLET_WALL, None, lo, hi,
+                 meta=dict(H=H, nu=nu, f=f, umax=umax, dx=dx, L=L, inlet=inlet, outlet=outlet, rules=rules))
+
+
 def poiseuille_ux_theory(y, t, H, nu, f, order=10):
     """Transient plane Poiseuille profile (the series of PoiseuilleFlow2D.jl:28-35)."""
     y = np.asarray(y, dtype=np.float64)

@@ -85,6 +85,7 @@ class Simulation:
         _abi.check(self.lib, None, self.lib.sph_create(C.byref(params), fluid_capacity, max(wall_capacity, 0),
                                                        C.byref(h)))
         self.h = h
+        self._fluid_capacity = fluid_capacity
 
     # -- lifetime
     def close(self):
@@ -130,6 +131,36 @@ class Simulation:
         self._check(self.lib.sph_upload_walls(self.h, kind, n, _abi.dptr(f(walls.x_vec_)),
                                               _abi.dptr(f(walls.normal_vec_)), _abi.dptr(f(walls.gap_)),
                                               _abi.dptr(t), _abi.dptr(kap), _abi.dptr(v)))
+
+    # -- inlet/outlet buffers (SPH_SOLVE_FLUID_INLET_OUTLET_WALL)
+    def upload_buffers(self, rules, inlet, outlet, capacity: int | None = None) -> None:
+        """Inlet and outlet particles (CommonLiquidParticles) and the transfer rules
+        (InletOutletRules); capacity: room for all buffer particles (default: inlet +
+        outlet + as many as the fluid)."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        cap = capacity if capacity is not None else len(inlet) + len(outlet) + self._fluid_capacity
+        arrays = lambda g: [_abi.dptr(f(getattr(g, k))) for k in ("x_vec_", "v_vec_", "rho_", "p_", "c_", "mass_",
+                                                                   "gap_")]
+        r = rules.c_struct()
+        self._keep = (inlet, outlet)
+        self._check(self.lib.sph_upload_buffers(self.h, C.byref(r), cap, len(inlet), *arrays(inlet), len(outlet),
+                                                *arrays(outlet)))
+
+    def download_buffers(self, which: int) -> dict:
+        """Inlet (0) or outlet (1) particles in the reference's vector order."""
+        n = C.c_int64()
+        self.lib.sph_download_buffers(self.h, which, 0, C.byref(n), *([None] * 7))  # the count
+        out = {k: np.empty((n.value, self.dim)) for k in ("x", "v")}
+        for k in ("rho", "p", "c", "mass", "gap"):
+            out[k] = np.empty(n.value)
+        names = ("x", "v", "rho", "p", "c", "mass", "gap")
+        self._check(self.lib.sph_download_buffers(self.h, which, n.value, C.byref(n),
+                                                  *[_abi.dptr(out[k]) for k in names]))
+        return out
+
+    def set_buffer_velocity(self, which: int, v) -> None:
+        vv = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, self.dim)
+        self._check(self.lib.sph_set_buffer_velocity(self.h, which, len(vv), vv.ctypes.data))
 
     def step(self, first_step: int, nsteps: int) -> None:
         self._check(self.lib.sph_step(self.h, first_step, nsteps))

@@ -236,3 +236,34 @@ class AABBCheck:
         lo = np.asarray(self.lo[:d])
         hi = np.asarray(self.hi[:d])
         return ~np.any((x > hi) | (x < lo), axis=1)
+
+
+@dataclass(frozen=True)
+class InletOutletRules:
+    """The keyword closures of the inlet/outlet solve! (FluidInletOutletWallSolve.jl:
+    inlet_into_calculation_domain_check, inlet_into_calculation_domain_modify,
+    outlet_out_calculation_domain_check, outlet_out_check) as the plane tests the
+    example's closures are (PoiseuilleFlow2D.jl:146-151): a particle passes when
+    normal . x > offset; an inlet particle that entered the fluid is moved by
+    inlet_shift."""
+
+    inlet_normal: tuple
+    inlet_offset: float
+    inlet_shift: tuple
+    outlet_normal: tuple
+    outlet_offset: float
+    drop_normal: tuple
+    drop_offset: float
+
+    def c_struct(self):
+        from . import _abi
+        pad = lambda v: tuple(float(a) for a in v) + (0.0,) * (3 - len(v))
+        r = _abi.SphBufferRules()
+        r.inlet_normal[:] = pad(self.inlet_normal)
+        r.inlet_offset = float(self.inlet_offset)
+        r.inlet_shift[:] = pad(self.inlet_shift)
+        r.outlet_normal[:] = pad(self.outlet_normal)
+        r.outlet_offset = float(self.outlet_offset)
+        r.drop_normal[:] = pad(self.drop_normal)
+        r.drop_offset = float(self.drop_offset)
+        return r

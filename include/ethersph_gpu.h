@@ -66,7 +66,8 @@ enum {
     SPH_SOLVE_FLUID_WALL = 0,                       /* FluidWallSolve.jl:8-83                       */
     SPH_SOLVE_FLUID_THERMOSTATIC_WALL = 1,          /* FluidThermostaticWallSolve.jl:8-125          */
     SPH_SOLVE_FLUID_COMPULSIVE_THERMOSTATIC_WALL = 2, /* FluidCompulsiveThermostaticWallSolve.jl:8-152 */
-    SPH_SOLVE_FLUID_VELOCITY_WALL = 3               /* FluidVelocitySolve.jl:8-102                  */
+    SPH_SOLVE_FLUID_VELOCITY_WALL = 3,              /* FluidVelocitySolve.jl:8-102                  */
+    SPH_SOLVE_FLUID_INLET_OUTLET_WALL = 4           /* FluidInletOutletWallSolve.jl:8-262           */
 };
 
 /* ---- wall particle types: src/Particle/FixedParticle/WallParticle.jl --------------- */
@@ -314,6 +315,52 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * against 1 the compiler's contraction of a*b+c into fused multiply-adds), never on the
  * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
+
+/* ---- inlet / outlet buffers ------------------------------------------------------
+ * FluidInletOutletWallSolve (src/Solve/FluidInletOutletWallSolve.jl:8-262), for a
+ * single-scene handle created with solve = SPH_SOLVE_FLUID_INLET_OUTLET_WALL (fluid,
+ * compulsive walls without wall pressure, no thermal model).  Inlet and outlet particles
+ * are fluid particles that enter the fluid's continuity and momentum sums as neighbours
+ * but are not updated by them: each step they move by x += v dt and keep rho, p, c.
+ * After the step (on the device, in the same kernels stream):
+ *   - an inlet particle with n_in.x > d_in is copied into the fluid (a new fluid particle
+ *     with the inlet particle's state; ids continue after the uploaded fluid, ordered by
+ *     step, then by inlet index, as push! orders them) and then moved by in_shift
+ *     (inlet_into_calculation_domain_check / _modify);
+ *   - a fluid particle with n_out.x > d_out moves to the outlet (it leaves the fluid:
+ *     outlet_out_calculation_domain_check);
+ *   - an outlet particle with n_drop.x > d_drop is removed (outlet_out_check).
+ * The examples' check functions compare one coordinate with a bound
+ * (PoiseuilleFlow2D.jl:146-151): n is then a unit axis.  user_defined_function, a host
+ * callback, becomes sph_set_buffer_velocity between step calls. */
+typedef struct SphBufferRules {
+    double inlet_normal[3];
+    double inlet_offset;
+    double inlet_shift[3];
+    double outlet_normal[3];
+    double outlet_offset;
+    double drop_normal[3];
+    double drop_offset;
+} SphBufferRules;
+
+/* Set the rules and the buffer particles (replaces earlier buffers): n_inlet inlet and
+ * n_outlet outlet particles (x, v: dim x n; rho, p, c, mass, gap: n), room for
+ * `capacity` buffer particles in all (the outlet grows by the fluid it receives). */
+int32_t sph_upload_buffers(SphHandle* h, const SphBufferRules* rules, int64_t capacity, int64_t n_inlet,
+                           const double* x, const double* v, const double* rho, const double* p, const double* c,
+                           const double* mass, const double* gap, int64_t n_outlet, const double* ox,
+                           const double* ov, const double* orho, const double* op, const double* oc,
+                           const double* omass, const double* ogap);
+
+/* Overwrite the velocities of the inlet (which = 0) or outlet (which = 1) particles, in
+ * their order (v: dim x n, n = their current count): the device counterpart of a
+ * user_defined_function that prescribes the buffer velocity between steps. */
+int32_t sph_set_buffer_velocity(SphHandle* h, int32_t which, int64_t n, const double* v);
+
+/* The inlet (which = 0) or outlet (which = 1) particles in the reference's vector order
+ * (inlet: upload order; outlet: uploaded ones, then arrivals by step and fluid order). */
+int32_t sph_download_buffers(SphHandle* h, int32_t which, int64_t capacity, int64_t* n_out, double* x, double* v,
+                             double* rho, double* p, double* c, double* mass, double* gap);
 
 /* ---- SPH interpolation at points (probes) --------------------------------------
  * kernelValueInterpolation (src/DataIO/VTPToDataFrame.jl:93-142) on the device state:

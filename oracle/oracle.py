@@ -58,6 +58,10 @@ def lib() -> C.CDLL:
         L.or_cell_keys.argtypes = [C.c_void_p, C.c_int64, _DP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.or_neighbour_counts.argtypes = [C.c_void_p, C.c_int64, _DP, C.c_int64, _DP, C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]
+        L.or_run_io.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_int64] + [_DP] * 7 + \
+            [C.c_int64, _DP, _DP, _DP, C.POINTER(C.c_int32), C.c_void_p, C.c_int64] + [_DP] * 7 + \
+            [C.POINTER(C.c_int64), C.c_int64] + [_DP] * 7 + [C.c_int64, C.c_int64, C.POINTER(C.c_int64)]
+        L.or_run_io.restype = C.c_int
         L.or_probe.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int64, _DP, C.c_int64, _DP,
                                _DP, _DP, C.c_int, C.POINTER(_DP), C.c_double, _DP]
         L.or_probe.restype = C.c_int
@@ -175,6 +179,47 @@ def probe(kind, dim, rc, points, x, mass, rho, fields, none_value=float("nan"), 
     if rc_ != 0:
         raise ValueError("bad kernel")
     return out
+
+
+def run_io(params, fluid: dict, walls: dict, rules, inlet: dict, outlet: dict, first_step: int, nsteps: int,
+           extra: int = 0):
+    """The inlet/outlet solve (gather mode): dicts of x, v (n, dim) and rho, p, c, mass,
+    gap; walls: x, normal, gap, kind; rules: an SphBufferRules.  Returns (fluid, inlet,
+    outlet) dicts in the reference's vector orders (fluid["id"]: ids, ascending).
+    `extra` = room for fluid and outlet growth."""
+    dim = params.dim
+    keys = ("rho", "p", "c", "mass", "gap")
+
+    def arrs(d, cap):
+        n = len(d["rho"])
+        out = {"x": np.zeros((cap, dim)), "v": np.zeros((cap, dim))}
+        out["x"][:n] = d["x"]
+        out["v"][:n] = d["v"]
+        for k in keys:
+            out[k] = np.zeros(cap)
+            out[k][:n] = d[k]
+        return n, out
+
+    nf, F = arrs(fluid, len(fluid["rho"]) + extra)
+    ni, I = arrs(inlet, len(inlet["rho"]))
+    no, O = arrs(outlet, len(outlet["rho"]) + extra)
+    wx = np.ascontiguousarray(walls["x"], dtype=np.float64)
+    wn = np.ascontiguousarray(walls["normal"], dtype=np.float64)
+    wg = np.ascontiguousarray(walls["gap"], dtype=np.float64)
+    wk = np.ascontiguousarray(walls["kind"], dtype=np.int32)
+    n_f, n_o = C.c_int64(nf), C.c_int64(no)
+    ids = np.zeros(len(F["rho"]), dtype=np.int64)
+    rc = lib().or_run_io(C.byref(params), C.byref(n_f), len(F["rho"]), *[_p(F[k]) for k in ("x", "v") + keys],
+                         len(wg), _p(wx), _p(wn), _p(wg), wk.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(rules), ni,
+                         *[_p(I[k]) for k in ("x", "v") + keys], C.byref(n_o), len(O["rho"]),
+                         *[_p(O[k]) for k in ("x", "v") + keys], first_step, nsteps,
+                         ids.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc != 0:
+        raise ValueError(f"or_run_io failed ({rc})")
+    cut = lambda d, n: {k: a[:n].copy() for k, a in d.items()}
+    fl = cut(F, n_f.value)
+    fl["id"] = ids[: n_f.value].copy()
+    return fl, cut(I, ni), cut(O, n_o.value)
 
 
 def scene_arrays(scene):

@@ -10,7 +10,8 @@
 //   src/Neighbour/Neighbour.jl
 //   src/ParticleAction/Interaction/*.jl, SelfAction/*.jl, GroupAction/ReconstructValue.jl
 //   src/Solve/{FluidWallSolve,FluidThermostaticWallSolve,
-//              FluidCompulsiveThermostaticWallSolve,FluidVelocitySolve}.jl (eachStep!)
+//              FluidCompulsiveThermostaticWallSolve,FluidVelocitySolve,
+//              FluidInletOutletWallSolve}.jl (eachStep!)
 //
 // Two summation modes:
 //   ORACLE_SCATTER: a half pair list (i<j, the CellListMap convention) with
@@ -428,7 +429,8 @@ void wall_terms(const Grid& G, const Kern& K, const Model& M, const double* xi, 
         }
     }
     // background pressure against the wall
-    if (M.solve != SPH_SOLVE_FLUID_WALL) {
+    // (neither in the inlet/outlet solve, FluidInletOutletWallSolve.jl:121-124)
+    if (M.solve != SPH_SOLVE_FLUID_WALL && M.solve != SPH_SOLVE_FLUID_INLET_OUTLET_WALL) {
         double prho2 = pi_ / (rhoi * rhoi) + M.p0 / (M.rho0 * M.rho0);
         prho2 += std::fabs(prho2) * 0.01 * P.W / kernel_value(gapi, K);
         for (int k = 0; k < dim; ++k) dvi[k] += -mi * prho2 * P.g[k];
@@ -794,6 +796,240 @@ void step_gather(const Grid& G, const Kern& K, const Model& M, Fluid& F, const W
     if (M.check_enabled && M.check_interval > 0 && step % M.check_interval == 0) delete_outside(F, M);
 }
 
+// ---------------------------------------------------------------- inlet / outlet
+// FluidInletOutletWallSolve.jl:8-262 in gather mode.  Buffer particles (inlet and
+// outlet) are neighbours of the fluid in continuity and momentum with their own, frozen
+// rho, p, c; after the step they move by x += v dt (updatePosition! with dv = 0).  The
+// closures of the reference's keywords are restated as plane tests n.x > d (what the
+// example's closures express, PoiseuilleFlow2D.jl:146-151), the modify closure as a
+// shift.  Visiting order: fluid neighbours, then buffer neighbours (cells z, y, x; inside
+// a cell by order), then walls, as the GPU sums them.
+constexpr int64_t kOutletBit = int64_t(1) << 62;
+
+struct Buffers {
+    int64_t n = 0;
+    std::vector<double> x, v, rho, p, c, m, gap;
+    std::vector<int64_t> order;  // inlet k: k; outlet: kOutletBit | ...
+};
+
+struct BufRules {
+    double in_n[3], in_d, in_shift[3], out_n[3], out_d, drop_n[3], drop_d;
+    int64_t n_inlet, id_base, first_step;
+};
+
+bool beyond(const double* n, double d, const double* x, int dim) {
+    double s = n[0] * x[0];
+    for (int k = 1; k < dim; ++k) s = s + n[k] * x[k];
+    return s > d;
+}
+
+void permute_buffers(Buffers& B, const std::vector<int64_t>& order, int dim) {
+    const int64_t n = B.n;
+    auto p1 = [&](std::vector<double>& a) {
+        std::vector<double> b(n);
+        for (int64_t k = 0; k < n; ++k) b[k] = a[order[k]];
+        a.swap(b);
+    };
+    auto pd = [&](std::vector<double>& a) {
+        std::vector<double> b((size_t)n * dim);
+        for (int64_t k = 0; k < n; ++k)
+            for (int q = 0; q < dim; ++q) b[k * dim + q] = a[order[k] * dim + q];
+        a.swap(b);
+    };
+    pd(B.x); pd(B.v);
+    p1(B.rho); p1(B.p); p1(B.c); p1(B.m); p1(B.gap);
+    std::vector<int64_t> o(n);
+    for (int64_t k = 0; k < n; ++k) o[k] = B.order[order[k]];
+    B.order.swap(o);
+}
+
+void step_gather_io(const Grid& G, const Kern& K, const Model& M, Fluid& F, const Walls& W, const CellList& WL,
+                    Buffers& B, const BufRules& R, int64_t step) {
+    const int dim = K.dim;
+    const double rc2 = K.rc * K.rc;
+    {
+        CellList tmp = build_cells(G, F.n, F.x.data(), dim, F.id.data());
+        permute(F, tmp.order, dim);
+        CellList tb = build_cells(G, B.n, B.x.data(), dim, B.order.data());
+        permute_buffers(B, tb.order, dim);
+    }
+    const int64_t n = F.n;
+    CellList CL = build_cells(G, n, F.x.data(), dim, F.id.data());
+    CellList BL = build_cells(G, B.n, B.x.data(), dim, B.order.data());
+    std::vector<double> x0(F.x), v0(F.v);
+    // continuity: fluid, then buffer neighbours (FluidInletOutletWallSolve.jl:59-72)
+    for (int64_t i = 0; i < n; ++i) {
+        const double* xi = &x0[i * dim];
+        int64_t c[3];
+        cell_of(G, xi, c);
+        int64_t cells[kMaxCells];
+        const int nc = neighbour_cells(G, c, cells);
+        double drho = 0.0;
+        for (int q = 0; q < nc; ++q)
+            for (int64_t j = CL.start[cells[q]]; j < CL.start[cells[q] + 1]; ++j) {
+                if (j == i) continue;
+                double rv[3];
+                rvec(G, xi, &x0[j * dim], dim, rv);
+                const double d2 = dist2(rv, dim);
+                if (!(d2 <= rc2)) continue;
+                PairGeom P;
+                pair_geom(G, K, xi, &x0[j * dim], &v0[i * dim], &v0[j * dim], d2, &P);
+                drho += dotv(P.vv, P.g, dim) * F.m[j];
+            }
+        for (int q = 0; q < nc; ++q)
+            for (int64_t b = BL.start[cells[q]]; b < BL.start[cells[q] + 1]; ++b) {
+                double rv[3];
+                rvec(G, xi, &B.x[b * dim], dim, rv);
+                const double d2 = dist2(rv, dim);
+                if (!(d2 <= rc2)) continue;
+                PairGeom P;
+                pair_geom(G, K, xi, &B.x[b * dim], &v0[i * dim], &B.v[b * dim], d2, &P);
+                drho += dotv(P.vv, P.g, dim) * B.m[b];
+            }
+        F.drho[i] = drho;
+    }
+    for (int64_t i = 0; i < n; ++i) density_pressure(F, i, M);
+    // momentum: fluid, buffers (:125-158), walls (wallForce! + viscosity, :111-124)
+    for (int64_t i = 0; i < n; ++i) {
+        const double* xi = &x0[i * dim];
+        int64_t c[3];
+        cell_of(G, xi, c);
+        int64_t cells[kMaxCells];
+        const int nc = neighbour_cells(G, c, cells);
+        double dv[3] = {0, 0, 0}, dT = 0.0;
+        for (int q = 0; q < nc; ++q)
+            for (int64_t j = CL.start[cells[q]]; j < CL.start[cells[q] + 1]; ++j) {
+                if (j == i) continue;
+                double rv[3];
+                rvec(G, xi, &x0[j * dim], dim, rv);
+                const double d2 = dist2(rv, dim);
+                if (!(d2 <= rc2)) continue;
+                PairGeom P;
+                pair_geom(G, K, xi, &x0[j * dim], &v0[i * dim], &v0[j * dim], d2, &P);
+                pressure_ff(F.p[i], F.rho[i], F.p[j], F.rho[j], F.gap[i], F.gap[j], F.m[j], P, K, dv);
+                viscosity_ff(F.rho[i], F.rho[j], F.m[j], P, K, M, dv);
+            }
+        for (int q = 0; q < nc; ++q)
+            for (int64_t b = BL.start[cells[q]]; b < BL.start[cells[q] + 1]; ++b) {
+                double rv[3];
+                rvec(G, xi, &B.x[b * dim], dim, rv);
+                const double d2 = dist2(rv, dim);
+                if (!(d2 <= rc2)) continue;
+                PairGeom P;
+                pair_geom(G, K, xi, &B.x[b * dim], &v0[i * dim], &B.v[b * dim], d2, &P);
+                pressure_ff(F.p[i], F.rho[i], B.p[b], B.rho[b], F.gap[i], B.gap[b], B.m[b], P, K, dv);
+                viscosity_ff(F.rho[i], B.rho[b], B.m[b], P, K, M, dv);
+            }
+        if (W.n > 0)
+            for (int q = 0; q < nc; ++q)
+                for (int64_t s = WL.start[cells[q]]; s < WL.start[cells[q] + 1]; ++s) {
+                    const int64_t w = WL.order[s];
+                    double rv[3];
+                    rvec(G, xi, &W.x[w * dim], dim, rv);
+                    const double d2 = dist2(rv, dim);
+                    if (!(d2 <= rc2)) continue;
+                    wall_terms(G, K, M, xi, &v0[i * dim], F.rho[i], F.p[i], F.c[i], F.m[i], F.gap[i], F.T[i],
+                               F.kappa[i], W, w, d2, dv, &dT);
+                }
+        for (int k = 0; k < dim; ++k) F.dv[i * dim + k] = dv[k];
+    }
+    for (int64_t i = 0; i < n; ++i) integrate(F, i, M, G);
+    if (M.reinit_interval > 0 && step % M.reinit_interval == 0) {  // fluid neighbours only
+        std::vector<double> rho_new(n);
+        for (int64_t i = 0; i < n; ++i) {
+            const double* xi = &x0[i * dim];
+            int64_t c[3];
+            cell_of(G, xi, c);
+            int64_t cells[kMaxCells];
+            const int nc = neighbour_cells(G, c, cells);
+            double sw = 0.0, sws = 0.0;
+            for (int q = 0; q < nc; ++q)
+                for (int64_t j = CL.start[cells[q]]; j < CL.start[cells[q] + 1]; ++j) {
+                    if (j == i) continue;
+                    double rv[3];
+                    rvec(G, xi, &x0[j * dim], dim, rv);
+                    const double d2 = dist2(rv, dim);
+                    if (!(d2 <= rc2)) continue;
+                    const double Wij = kernel_value(std::sqrt(d2), K);
+                    sw += Wij * F.m[j] / F.rho[j];
+                    sws += Wij * F.m[j] / F.rho[j] * F.rho[j];
+                }
+            sw += K.k0 * F.m[i] / F.rho[i];
+            sws += K.k0 * F.m[i] / F.rho[i] * F.rho[i];
+            rho_new[i] = sws / sw;
+        }
+        std::copy(rho_new.begin(), rho_new.end(), F.rho.begin());
+    }
+    if (M.check_enabled && M.check_interval > 0 && step % M.check_interval == 0) delete_outside(F, M);
+    // transfers (:162-257), decided on the state at the end of the step
+    const int64_t srel = step - R.first_step;
+    std::vector<char> to_outlet(F.n, 0);
+    for (int64_t i = 0; i < F.n; ++i) to_outlet[i] = beyond(R.out_n, R.out_d, &F.x[i * dim], dim);
+    Buffers NB;  // buffers after the move: survivors in place, then the fluid arrivals
+    Fluid add;   // fluid copies of inlet particles
+    for (int64_t b = 0; b < B.n; ++b) {
+        double xn[3];
+        for (int k = 0; k < dim; ++k) xn[k] = B.x[b * dim + k] + B.v[b * dim + k] * M.dt;
+        if (!(B.order[b] & kOutletBit)) {
+            if (beyond(R.in_n, R.in_d, xn, dim)) {
+                for (int k = 0; k < dim; ++k) {
+                    add.x.push_back(xn[k]);
+                    add.v.push_back(B.v[b * dim + k]);
+                }
+                add.rho.push_back(B.rho[b]); add.p.push_back(B.p[b]); add.c.push_back(B.c[b]);
+                add.m.push_back(B.m[b]); add.gap.push_back(B.gap[b]);
+                add.id.push_back(R.id_base + srel * R.n_inlet + B.order[b]);
+                ++add.n;
+                for (int k = 0; k < dim; ++k) xn[k] += R.in_shift[k];
+            }
+        } else if (beyond(R.drop_n, R.drop_d, xn, dim)) {
+            continue;  // out of the outlet
+        }
+        for (int k = 0; k < dim; ++k) {
+            NB.x.push_back(xn[k]);
+            NB.v.push_back(B.v[b * dim + k]);
+        }
+        NB.rho.push_back(B.rho[b]); NB.p.push_back(B.p[b]); NB.c.push_back(B.c[b]);
+        NB.m.push_back(B.m[b]); NB.gap.push_back(B.gap[b]); NB.order.push_back(B.order[b]);
+        ++NB.n;
+    }
+    Fluid keep;
+    for (int64_t i = 0; i < F.n; ++i) {
+        if (to_outlet[i]) {
+            for (int k = 0; k < dim; ++k) {
+                NB.x.push_back(F.x[i * dim + k]);
+                NB.v.push_back(F.v[i * dim + k]);
+            }
+            NB.rho.push_back(F.rho[i]); NB.p.push_back(F.p[i]); NB.c.push_back(F.c[i]);
+            NB.m.push_back(F.m[i]); NB.gap.push_back(F.gap[i]);
+            NB.order.push_back(kOutletBit | ((srel + 1) << 32) | F.id[i]);
+            ++NB.n;
+            continue;
+        }
+        for (int k = 0; k < dim; ++k) {
+            keep.x.push_back(F.x[i * dim + k]);
+            keep.v.push_back(F.v[i * dim + k]);
+        }
+        keep.rho.push_back(F.rho[i]); keep.p.push_back(F.p[i]); keep.c.push_back(F.c[i]);
+        keep.m.push_back(F.m[i]); keep.gap.push_back(F.gap[i]); keep.id.push_back(F.id[i]);
+        ++keep.n;
+    }
+    for (int64_t a = 0; a < add.n; ++a) {
+        for (int k = 0; k < dim; ++k) {
+            keep.x.push_back(add.x[a * dim + k]);
+            keep.v.push_back(add.v[a * dim + k]);
+        }
+        keep.rho.push_back(add.rho[a]); keep.p.push_back(add.p[a]); keep.c.push_back(add.c[a]);
+        keep.m.push_back(add.m[a]); keep.gap.push_back(add.gap[a]); keep.id.push_back(add.id[a]);
+        ++keep.n;
+    }
+    F.n = keep.n;
+    F.x.swap(keep.x); F.v.swap(keep.v); F.rho.swap(keep.rho); F.p.swap(keep.p); F.c.swap(keep.c);
+    F.m.swap(keep.m); F.gap.swap(keep.gap); F.id.swap(keep.id);
+    F.T.assign(F.n, 0.0); F.kappa.assign(F.n, 0.0); F.cp.assign(F.n, 0.0);
+    B = NB;
+}
+
 bool load_model(const SphParams* p, Model* M, Kern* K) {
     if (!p || (p->dim != 2 && p->dim != 3)) return false;
     if (!make_kernel(p->kernel, p->dim, p->influence_radius, K)) return false;
@@ -1028,6 +1264,104 @@ int or_run(const SphParams* prm, int mode, int threads, int64_t* n_fluid, double
         std::copy(F.T.begin(), F.T.begin() + F.n, t);
         std::copy(F.kappa.begin(), F.kappa.begin() + F.n, kappa);
         std::copy(F.cp.begin(), F.cp.begin() + F.n, cp);
+    }
+    return 0;
+}
+
+// The inlet/outlet solve in gather mode.  Fluid (x, v: dim x cap; rho, p, c, mass,
+// gap: cap) is replaced by the fluid at the end, in ascending id (uploaded ids 0..n-1,
+// inlet copies after them); inlet arrays (n_in) by the inlet particles in index order;
+// outlet arrays (capacity out_cap) by the outlet particles in arrival order; ids_out (cap)
+// receives the fluid ids.  Returns 1 on bad parameters, 2 when a capacity is too small.
+int or_run_io(const SphParams* prm, int64_t* n_fluid, int64_t cap, double* x, double* v, double* rho, double* p,
+              double* c, double* mass, double* gap, int64_t n_wall, const double* wx, const double* wnormal,
+              const double* wgap, const int32_t* wkind, const SphBufferRules* rules, int64_t n_in, double* ix,
+              double* iv, double* irho, double* ip, double* ic, double* imass, double* igap, int64_t* n_out,
+              int64_t out_cap, double* ox, double* ov, double* orho, double* op, double* oc, double* omass,
+              double* ogap, int64_t first_step, int64_t nsteps, int64_t* ids_out) {
+    Model M;
+    Kern K;
+    if (!load_model(prm, &M, &K) || M.thermal || !rules) return 1;
+    const int dim = M.dim;
+    Grid G = make_grid(M, K.rc);
+    Fluid F;
+    const int64_t n = *n_fluid;
+    F.n = n;
+    F.x.assign(x, x + n * dim); F.v.assign(v, v + n * dim);
+    F.rho.assign(rho, rho + n); F.p.assign(p, p + n); F.c.assign(c, c + n);
+    F.m.assign(mass, mass + n); F.gap.assign(gap, gap + n);
+    F.T.assign(n, 0.0); F.kappa.assign(n, 0.0); F.cp.assign(n, 0.0);
+    F.id.resize(n);
+    for (int64_t i = 0; i < n; ++i) F.id[i] = i;
+    Walls W;
+    W.n = n_wall;
+    if (n_wall > 0) {
+        W.x.assign(wx, wx + n_wall * dim);
+        W.nrm.assign(wnormal, wnormal + n_wall * dim);
+        W.gap.assign(wgap, wgap + n_wall);
+        W.T.assign(n_wall, 0.0);
+        W.kappa.assign(n_wall, 0.0);
+        W.v.assign(n_wall * dim, 0.0);
+        W.kind.assign(wkind, wkind + n_wall);
+    }
+    std::vector<int64_t> wid(n_wall);
+    for (int64_t w = 0; w < n_wall; ++w) wid[w] = w;
+    CellList WL = build_cells(G, n_wall, W.x.data(), dim, wid.data());
+    Buffers B;
+    const int64_t no = *n_out;
+    B.n = n_in + no;
+    for (int64_t b = 0; b < n_in; ++b) {
+        for (int k = 0; k < dim; ++k) { B.x.push_back(ix[b * dim + k]); B.v.push_back(iv[b * dim + k]); }
+        B.rho.push_back(irho[b]); B.p.push_back(ip[b]); B.c.push_back(ic[b]); B.m.push_back(imass[b]);
+        B.gap.push_back(igap[b]); B.order.push_back(b);
+    }
+    for (int64_t b = 0; b < no; ++b) {
+        for (int k = 0; k < dim; ++k) { B.x.push_back(ox[b * dim + k]); B.v.push_back(ov[b * dim + k]); }
+        B.rho.push_back(orho[b]); B.p.push_back(op[b]); B.c.push_back(oc[b]); B.m.push_back(omass[b]);
+        B.gap.push_back(ogap[b]); B.order.push_back(kOutletBit | b);
+    }
+    BufRules R;
+    for (int k = 0; k < 3; ++k) {
+        R.in_n[k] = rules->inlet_normal[k]; R.in_shift[k] = rules->inlet_shift[k];
+        R.out_n[k] = rules->outlet_normal[k]; R.drop_n[k] = rules->drop_normal[k];
+    }
+    R.in_d = rules->inlet_offset; R.out_d = rules->outlet_offset; R.drop_d = rules->drop_offset;
+    R.n_inlet = n_in; R.id_base = n; R.first_step = first_step;
+    for (int64_t s = first_step; s < first_step + nsteps; ++s) {
+        F.drho.assign(F.n, 0.0); F.dv.assign(F.n * dim, 0.0); F.dT.assign(F.n, 0.0);
+        F.sw.assign(F.n, 0.0); F.sws.assign(F.n, 0.0);
+        step_gather_io(G, K, M, F, W, WL, B, R, s);
+    }
+    std::vector<int64_t> ord(F.n);
+    for (int64_t k = 0; k < F.n; ++k) ord[k] = k;
+    std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return F.id[a] < F.id[b]; });
+    permute(F, ord, dim);
+    std::vector<int64_t> bo(B.n);
+    for (int64_t k = 0; k < B.n; ++k) bo[k] = k;
+    std::sort(bo.begin(), bo.end(), [&](int64_t a, int64_t b) { return B.order[a] < B.order[b]; });
+    permute_buffers(B, bo, dim);
+    int64_t n_inlet_end = 0;
+    while (n_inlet_end < B.n && !(B.order[n_inlet_end] & kOutletBit)) ++n_inlet_end;
+    const int64_t n_outlet_end = B.n - n_inlet_end;
+    *n_fluid = F.n;
+    *n_out = n_outlet_end;
+    if (F.n > cap || n_outlet_end > out_cap || n_inlet_end != n_in) return 2;
+    std::copy(F.x.begin(), F.x.end(), x); std::copy(F.v.begin(), F.v.end(), v);
+    std::copy(F.rho.begin(), F.rho.end(), rho); std::copy(F.p.begin(), F.p.end(), p);
+    std::copy(F.c.begin(), F.c.end(), c); std::copy(F.m.begin(), F.m.end(), mass);
+    std::copy(F.gap.begin(), F.gap.end(), gap);
+    if (ids_out) std::copy(F.id.begin(), F.id.end(), ids_out);
+    for (int64_t b = 0; b < B.n; ++b) {
+        const bool in = b < n_inlet_end;
+        const int64_t q = in ? b : b - n_inlet_end;
+        double* xs = in ? ix : ox;
+        double* vs = in ? iv : ov;
+        for (int k = 0; k < dim; ++k) { xs[q * dim + k] = B.x[b * dim + k]; vs[q * dim + k] = B.v[b * dim + k]; }
+        (in ? irho : orho)[q] = B.rho[b];
+        (in ? ip : op)[q] = B.p[b];
+        (in ? ic : oc)[q] = B.c[b];
+        (in ? imass : omass)[q] = B.m[b];
+        (in ? igap : ogap)[q] = B.gap[b];
     }
     return 0;
 }
