@@ -6,7 +6,7 @@ include/ethersph_gpu.h); this package mirrors the reference's type tree and its
 """
 from . import _abi
 from ._abi import SphError, SphParams, SphStats, load_library
-from .solver import Simulation, kernelValueInterpolation, make_params, solve
+from .solver import Simulation, kernelValueInterpolation, make_params, solve, solve_inlet_outlet
 from .batch import Batch
 from .vtp import VTPIO
 from .types import (AABBCheck, CommonLiquidParticles, CommonWeaklyCompressibleLiquidModel, CompulsiveWallParticles,

@@ -27,7 +27,8 @@ module EtherSPHGPU
 
 using EtherSPHCPU
 
-export GPU, FP64, FP32Compensated, GPUScene, GPUBatch, SceneRequest, serve, step!, download!, probe
+export GPU, FP64, FP32Compensated, GPUScene, GPUBatch, SceneRequest, serve, step!, download!, probe, PlaneRules,
+       setBufferVelocity!
 
 const libsph = joinpath(@__DIR__, "..", "lib", "libethersph_gpu.so")
 
@@ -261,6 +262,151 @@ function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidPartic
     staged_output::Bool = true)::Nothing
     return runSolve!(Int32(2), fluid_particles, [wall_particles, thermostatic_wall_particles], smooth_kernel,
         th_wc_lm, dr_fti_forward_euler, vtp_io, check, aabb, precision, domain, false, staged_output)
+end
+
+# ---------------------------------------------------------------- inlet / outlet
+# Mirror of SphBufferRules (include/ethersph_gpu.h).
+struct SphBufferRules
+    inlet_normal::NTuple{3, Float64}
+    inlet_offset::Float64
+    inlet_shift::NTuple{3, Float64}
+    outlet_normal::NTuple{3, Float64}
+    outlet_offset::Float64
+    drop_normal::NTuple{3, Float64}
+    drop_offset::Float64
+end
+
+"""
+    PlaneRules(; inlet = (normal, offset), shift, outlet = (normal, offset), drop = (normal, offset))
+
+The keyword closures of the inlet/outlet solve! as planes: a particle passes a check when
+normal . x > offset (inletIntoCalculationDomainCheck(p) = p.x_vec_[1] > x0 is
+inlet = ([1, 0], x0)); an inlet particle that entered the fluid moves by `shift`
+(inletIntoCalculationDomainModify).
+"""
+PlaneRules(; inlet, shift, outlet, drop) = SphBufferRules(pad3(inlet[1]), Float64(inlet[2]), pad3(shift),
+    pad3(outlet[1]), Float64(outlet[2]), pad3(drop[1]), Float64(drop[2]))
+
+function uploadBuffers(h, rules::SphBufferRules, inlet, outlet, capacity)
+    f(g, k) = isempty(g) ? Float64[] : (k === :x_vec_ || k === :v_vec_ ? stack(g, k) : Float64[getfield(p, k) for p in g])
+    checkStatus(h, ccall((:sph_upload_buffers, libsph), Int32,
+        (Ptr{Cvoid}, Ref{SphBufferRules}, Int64, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64,
+         Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h, Ref(rules), capacity, length(inlet), f(inlet, :x_vec_), f(inlet, :v_vec_), f(inlet, :rho_), f(inlet, :p_),
+        f(inlet, :c_), f(inlet, :mass_), f(inlet, :gap_), length(outlet), f(outlet, :x_vec_), f(outlet, :v_vec_),
+        f(outlet, :rho_), f(outlet, :p_), f(outlet, :c_), f(outlet, :mass_), f(outlet, :gap_)))
+end
+
+# The inlet (which = 0) or outlet (1) particles back into `group` (resized to the device's).
+function downloadBuffers!(h, which, group, dim)
+    n = Ref{Int64}(0)
+    ccall((:sph_download_buffers, libsph), Int32, (Ptr{Cvoid}, Int32, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h, Int32(which), 0, n, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL)  # the count
+    x, v = zeros(dim, n[]), zeros(dim, n[])
+    rho, p, c, m, gap = zeros(n[]), zeros(n[]), zeros(n[]), zeros(n[]), zeros(n[])
+    checkStatus(h, ccall((:sph_download_buffers, libsph), Int32,
+        (Ptr{Cvoid}, Int32, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h, Int32(which), n[], n, x, v, rho, p, c, m, gap))
+    proto = group[1]
+    while length(group) < n[]
+        push!(group, deepcopy(proto))
+    end
+    resize!(group, n[])
+    for (i, pt) in enumerate(group)
+        pt.x_vec_ .= view(x, :, i)
+        pt.v_vec_ .= view(v, :, i)
+        pt.rho_, pt.p_, pt.c_, pt.mass_, pt.gap_ = rho[i], p[i], c[i], m[i], gap[i]
+    end
+    return group
+end
+
+"""
+    setBufferVelocity!(h, which, v::Matrix{Float64})
+
+Overwrite the inlet (0) or outlet (1) velocities (dim x n, in their order): what the
+example's user_defined_function does between steps (PoiseuilleFlow2D.jl:152-167).
+"""
+setBufferVelocity!(h, which, v::AbstractMatrix) = checkStatus(h, ccall((:sph_set_buffer_velocity, libsph), Int32,
+    (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}), h, Int32(which), size(v, 2), Matrix{Float64}(v)))
+
+# FluidInletOutletWallSolve.jl:264-340.  user_defined_function(h, t) runs on the host
+# every `udf_interval` steps (the reference: after every step), with the handle for
+# setBufferVelocity!.
+function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidParticle},
+    inlet_fluid_particles::AbstractVector{<:FluidParticle}, outlet_fluid_particles::AbstractVector{<:FluidParticle},
+    wall_particles::AbstractVector{<:WallParticle}, smooth_kernel::SmoothKernel,
+    wc_lm::WeaklyCompressibleLiquidModel, dr_fti_forward_euler::DensityReinitializedFixedTimeIntervalForwardEuler,
+    vtp_io::VTPIO; rules::SphBufferRules, user_defined_function = nothing, udf_interval::Int = 1,
+    precision = FP64, domain = nothing, fluid_capacity::Int = 2 * length(fluid_particles) +
+    64 * length(inlet_fluid_particles), buffer_capacity::Int = length(inlet_fluid_particles) +
+    length(outlet_fluid_particles) + fluid_capacity)::Nothing
+    td = dr_fti_forward_euler
+    groups = [fluid_particles, inlet_fluid_particles, outlet_fluid_particles, wall_particles]
+    if domain === nothing
+        pts = reduce(hcat, [stack(g, :x_vec_) for g in groups if !isempty(g)])
+        pad = 2 * smooth_kernel.influence_radius_
+        domain = (vec(minimum(pts; dims = 2)) .- pad, vec(maximum(pts; dims = 2)) .+ pad)
+    end
+    prm = Ref(makeParams(smooth_kernel, wc_lm, td, Int32(4), precision, nothing, domain, false))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    checkStatus(C_NULL, ccall((:sph_create, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ref{Ptr{Cvoid}}),
+        prm, fluid_capacity, length(wall_particles), h))
+    dim = length(fluid_particles[1].x_vec_)
+    pull!() = begin
+        downloadFluidAll!(h[], fluid_particles)
+        downloadBuffers!(h[], 0, inlet_fluid_particles, dim)
+        downloadBuffers!(h[], 1, outlet_fluid_particles, dim)
+    end
+    try
+        uploadWalls(h[], wall_particles)
+        uploadFluid(h[], fluid_particles)
+        uploadBuffers(h[], rules, inlet_fluid_particles, outlet_fluid_particles, buffer_capacity)
+        assureDirPathExist(vtp_io)
+        writeVTP(0, 0.0, vtp_io, groups)
+        step = 1
+        while step <= td.total_step_
+            stop = step
+            while stop < td.total_step_ && stop % udf_interval != 0 && !isOutputStep(stop, td)
+                stop += 1
+            end
+            checkStatus(h[], ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), h[], step, stop - step + 1))
+            user_defined_function === nothing || user_defined_function(h[], stop * td.dt_)
+            if isOutputStep(stop, td)
+                pull!()
+                writeVTP(div(stop, td.output_interval_), stop * td.dt_, vtp_io, groups)
+            end
+            step = stop + 1
+        end
+        pull!()
+    finally
+        ccall((:sph_destroy, libsph), Int32, (Ptr{Cvoid},), h[])
+    end
+    return nothing
+end
+
+# The live fluid into the vector, growing it for particles that came from the inlet
+# (every field from the device, in ascending id).
+function downloadFluidAll!(h, fluid)
+    n = Ref{Int64}(0)
+    ccall((:sph_download_fluid, libsph), Int32, (Ptr{Cvoid}, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h, 0, n, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL)  # the count
+    dim = length(fluid[1].x_vec_)
+    x, v = zeros(dim, n[]), zeros(dim, n[])
+    rho, p, c, m, gap = zeros(n[]), zeros(n[]), zeros(n[]), zeros(n[]), zeros(n[])
+    checkStatus(h, ccall((:sph_download_fluid, libsph), Int32,
+        (Ptr{Cvoid}, Int64, Ref{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h, n[], n, x, v, rho, p, c, m, gap, C_NULL, C_NULL, C_NULL))
+    proto = fluid[1]
+    while length(fluid) < n[]
+        push!(fluid, deepcopy(proto))
+    end
+    resize!(fluid, n[])
+    for (i, pt) in enumerate(fluid)
+        pt.x_vec_ .= view(x, :, i)
+        pt.v_vec_ .= view(v, :, i)
+        pt.rho_, pt.p_, pt.c_, pt.mass_, pt.gap_ = rho[i], p[i], c[i], m[i], gap[i]
+    end
+    return fluid
 end
 
 # ---------------------------------------------------------------- a device-resident scene

@@ -333,6 +333,80 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
     return fluid
 
 
+def solve_inlet_outlet(fluid, inlet, outlet, walls, kernel, model, td, vtp_io=None, *, rules,
+                       user_defined_function=None, udf_interval: int = 1, precision: int = _abi.PRECISION_FP64,
+                       domain_lo=None, domain_hi=None, first_step: int = 1, nsteps: int | None = None,
+                       fluid_capacity: int | None = None, buffer_capacity: int | None = None,
+                       wall_time: str | None = None):
+    """GPU counterpart of the inlet/outlet solve!(fluid, inlet, outlet, walls, kernel,
+    model, td, vtp_io; checks..., user_defined_function) (FluidInletOutletWallSolve.jl:
+    264-340).  rules: InletOutletRules (the check/modify closures as planes).
+    user_defined_function(sim, t) runs on the host every `udf_interval` steps (the
+    reference calls it after every step, :258); it typically sets the buffer velocities
+    with sim.set_buffer_velocity.  VTP files hold [fluid, inlet, outlet, walls] (:282,
+    :331-336).  fluid, inlet and outlet are left holding the final state."""
+    if domain_lo is None or domain_hi is None:
+        pts = np.concatenate([g.x_vec_ for g in (fluid, inlet, outlet, walls) if len(g)])
+        pad = 2.0 * kernel.influence_radius_
+        domain_lo = pts.min(axis=0) - pad if domain_lo is None else domain_lo
+        domain_hi = pts.max(axis=0) + pad if domain_hi is None else domain_hi
+    params = make_params(kernel, model, td, solve=_abi.SOLVE_FLUID_INLET_OUTLET_WALL, precision=precision,
+                         domain_lo=list(domain_lo), domain_hi=list(domain_hi))
+    last = td.total_step_ if nsteps is None else first_step + nsteps - 1
+    # room for the fluid to grow while more enters than leaves (reported if exceeded)
+    cap = fluid_capacity if fluid_capacity is not None else 2 * len(fluid) + 64 * len(inlet)
+
+    def write(step_file, t):
+        if vtp_io is None:
+            return
+        _buffers_into(sim, inlet, 0)
+        _buffers_into(sim, outlet, 1)
+        _fluid_into(sim, fluid)
+        vtp_io.write(step_file, t, fluid, [inlet, outlet, walls], wall_time=wall_time)
+
+    with Simulation(params, cap, len(walls)) as sim:
+        sim.upload_walls(walls)
+        sim.upload_fluid(fluid)
+        sim.upload_buffers(rules, inlet, outlet, buffer_capacity)
+        write(0, 0.0)
+        step = first_step
+        while step <= last:
+            nxt = step
+            while nxt < last and (nxt - first_step + 1) % udf_interval != 0 and \
+                    not (vtp_io is not None and isOutputStep(nxt, td)):
+                nxt += 1
+            sim.step(step, nxt - step + 1)
+            step = nxt + 1
+            if user_defined_function is not None:
+                user_defined_function(sim, nxt * td.dt_)
+            if vtp_io is not None and isOutputStep(nxt, td):
+                write(nxt // td.output_interval_, nxt * td.dt_)
+        _fluid_into(sim, fluid)
+        _buffers_into(sim, inlet, 0)
+        _buffers_into(sim, outlet, 1)
+    return fluid, inlet, outlet
+
+
+def _fluid_into(sim, fluid):
+    """The live fluid into `fluid` (its length follows the device: the inlet adds)."""
+    _replace(fluid, sim.download(), sim.dim)
+
+
+def _buffers_into(sim, group, which):
+    _replace(group, sim.download_buffers(which), sim.dim)
+
+
+def _replace(group, d, dim):
+    n = len(d["rho"])
+    fresh = type(group)(n, dim)
+    fresh.x_vec_[:] = d["x"]
+    fresh.v_vec_[:] = d["v"]
+    for k, f in (("rho", "rho_"), ("p", "p_"), ("c", "c_"), ("mass", "mass_"), ("gap", "gap_")):
+        getattr(fresh, f)[:] = d[k]
+    for f in fresh._vector_fields + fresh._scalar_fields:
+        setattr(group, f, getattr(fresh, f))
+
+
 def kernelValueInterpolation(points, sim: Simulation, field, none_value: float = math.nan) -> np.ndarray:
     """Reference-named form of Simulation.probe for one field (VTPToDataFrame.jl:122-142):
     the interpolated values at `points` (n, dim) from the live fluid of `sim`."""

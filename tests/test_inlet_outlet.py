@@ -181,3 +181,41 @@ def scenes_fluid_wall(s):
     import dataclasses
     from ethersph_gb300 import _abi
     return dataclasses.replace(s, solve=_abi.SOLVE_FLUID_WALL)
+
+
+@pytest.mark.gpu
+def test_inlet_outlet_channel_follows_the_transient_profile(pkg, tmp_path):
+    # the reference example's protocol (PoiseuilleFlow2D.jl): the channel starts at rest,
+    # a callback sets the inlet and outlet particles to the analytic transient profile,
+    # the fluid in between is checked against that profile with a line probe
+    from ethersph_gb300 import scenes, vtp
+    s = scenes.poiseuille_inlet_outlet_2d(n_across=20, start="transient", total_step=1500)
+    m = s.meta
+
+    def udf(sim, t):
+        for which in (0, 1):
+            b = sim.download_buffers(which)
+            v = np.zeros_like(b["v"])
+            v[:, 0] = scenes.poiseuille_ux_theory(b["x"][:, 1], t, m["H"], m["nu"], m["f"])
+            sim.set_buffer_velocity(which, v)
+
+    io = vtp.VTPIO(2, "channel_", ".vtp", str(tmp_path), ["rho_", "p_"], ["Density", "Pressure"])
+    td = s.td
+    fluid, inlet, outlet = pkg.solve_inlet_outlet(s.fluid, m["inlet"], m["outlet"], s.walls[0], s.kernel, s.model,
+                                                  td, io, rules=m["rules"], user_defined_function=udf,
+                                                  udf_interval=10, domain_lo=s.domain_lo, domain_hi=s.domain_hi)
+    t = td.total_step_ * td.dt_
+    mid = (fluid.x_vec_[:, 0] > 0.4 * m["L"]) & (fluid.x_vec_[:, 0] < 0.6 * m["L"])
+    y, ux = fluid.x_vec_[mid, 1], fluid.v_vec_[mid, 0]
+    nominal = scenes.poiseuille_ux_theory(y, t, m["H"], m["nu"], m["f"])
+    # walls at dx/2 beyond the outermost fluid rows: the effective channel is H + dx wide
+    effective = scenes.poiseuille_ux_theory(y + m["dx"] / 2, t, m["H"] + m["dx"], m["nu"], m["f"])
+    err_nom = np.linalg.norm(ux - nominal) / np.linalg.norm(nominal)
+    err_eff = np.linalg.norm(ux - effective) / np.linalg.norm(effective)
+    print("inlet/outlet channel: t =", t, "L2 nominal", err_nom, "effective", err_eff, "fluid", len(fluid),
+          "outlet", len(outlet))
+    assert err_eff < 0.08 and err_nom < 0.1      # the oracle's restatement gives 0.052 / 0.072
+    assert len(inlet) == 3 * 20
+    last = vtp.read_vtp_arrays(str(tmp_path / "channel_15.vtp"))
+    assert set(np.unique(last["Type"])) == {1, 2, 3, 4}        # fluid, inlet, outlet, walls
+    assert int(np.sum(last["Type"] == 1)) == len(fluid)
