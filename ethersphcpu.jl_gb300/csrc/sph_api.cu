@@ -297,7 +297,7 @@ struct SphHandle {
     bool have_fluid = false;
     int64_t steps_done = 0;
     // FP32 launch shape: lanes per particle for continuity, momentum, Shepard; block size
-    int tune[4] = {4, 4, 4, 128};
+    int tune[4] = {1, 1, 1, 128};  // the autotuner's most frequent pick on large 2D and 3D scenes
     std::string err;
     std::vector<SceneRec> scenes;
     RangeAlloc cells, walls;

@@ -81,11 +81,15 @@ def summarize_ranks(report: Report, world: int = 1) -> dict:
 class Server:
     def __init__(self, budget_bytes: float = 150e9, precision: int = _abi.PRECISION_FP32_COMPENSATED,
                  share_3d: float = 0.4, bundle: int = 10, scene_capacity: int = 4096, keep_results: bool = False,
-                 launch_shape=None, lib=None):
+                 launch_shape=None, autotune: bool = False, lib=None):
         from . import scenes
         self.bundle = bundle
         self.precision = precision
         self.keep_results = keep_results
+        # re-tune a batch's launch shape (sph_autotune) whenever its live particles have
+        # doubled since the last tuning; off by default, because the FP32 form's results
+        # depend on the shape and a served result should equal the same scene run alone
+        self.autotune = autotune and launch_shape is None and precision == _abi.PRECISION_FP32_COMPENSATED
         proto2 = scenes.dam_break_2d(dx=0.05).params(precision=precision)
         proto3 = scenes.dam_break_3d(dx=0.05, tank=(0.4, 0.2, 0.4), column=(0.1, 0.1, 0.2)).params(precision=precision)
         self.batches = {
@@ -106,6 +110,7 @@ class Server:
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrival))
         queues = {2: collections.deque(), 3: collections.deque()}
         active = {}  # (dim, sid) -> [request, t_admit, steps_left, n_fluid]
+        tuned_at = {2: 0, 3: 0}
         done = []
         particle_steps = 0
         t0 = time.perf_counter()
@@ -133,6 +138,12 @@ class Server:
                 if pending:
                     time.sleep(max(0.0, min(0.01, pending[0].t_arrival - (time.perf_counter() - t0))))
                 continue
+            if self.autotune:
+                for dim, b in self.batches.items():
+                    live = sum(rec[3] for (d, _sid), rec in active.items() if d == dim)
+                    if live >= 20_000 and live >= 2 * tuned_at[dim]:
+                        b.autotune(2)
+                        tuned_at[dim] = live
             # one bundle of steps for every resident scene (both batches, overlapping)
             running = {dim for (dim, _sid) in active}
             for dim in running:

@@ -306,7 +306,8 @@ int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double
  * which keeps one thread per particle so that its summation order is fixed. */
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 
-/* Set the FP32 launch shape by hand: shape[4] = (continuity lanes, momentum lanes,
+/* Set the FP32 launch shape by hand (a new handle starts at (1, 1, 1, 128)):
+ * shape[4] = (continuity lanes, momentum lanes,
  * Shepard lanes, block size); lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
  * is software-pipelined: loads of the next neighbour overlap the current one's
  * arithmetic; momentum lanes -1 take blocks of at most 256), block in {32, 64, ..., 1024}
