@@ -398,8 +398,8 @@ def run_batched(args, rank=0, world=1):
     sc = distributed.shard(every, rank, world)
     nf = sum(s.n_fluid for s in sc)
     nw = sum(s.n_wall for s in sc)
-    nc = sum(batch.footprint(s, 1)[1] for s in sc)          # FP32 form (cells of r_cut)
-    nc64 = sum(batch.footprint(s, 0)[1] for s in sc)        # FP64 form (cells of r_cut / 2)
+    nc = sum(batch.footprint(s, 1)[1] for s in sc)          # FP32 form
+    nc64 = sum(batch.footprint(s, 0)[1] for s in sc)        # FP64 form
     nf_all = sum(s.n_fluid for s in every)
     res = {"workload": f"512 batched 2D dam breaks, {nf_all} fluid + {sum(s.n_wall for s in every)} wall "
                        "particles, CubicSpline, FluidWallSolve, per-scene c0 and dt", "fluid_particles": nf_all,

@@ -40,10 +40,8 @@ def merged_walls(scene):
 
 
 def cells_per_cutoff(cell_subdivision: int, precision: int, dim: int) -> int:
-    """The library's cell subdivision (its default: 1 for the FP32 form in 2D, else 2)."""
-    if cell_subdivision:
-        return cell_subdivision
-    return 1 if precision == _abi.PRECISION_FP32_COMPENSATED and dim == 2 else 2
+    """The library's cell subdivision (its default: 2 cells per r_cut)."""
+    return cell_subdivision if cell_subdivision else 2
 
 
 def grid_cells(scene, cell_subdivision: int = 0, precision: int = _abi.PRECISION_FP64) -> int:

@@ -90,10 +90,10 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
         err = "influence_radius, h, dt and rho_0 must be positive"; return false;
     }
     const double rc = p.influence_radius;
-    // cells per r_cut; default: 2 (fewer candidate pairs) except for the FP32 form in 2D,
-    // where the cheap candidate test makes the longer cell walk the larger cost
-    const int m = p.cell_subdivision != 0 ? p.cell_subdivision
-                                          : (p.precision == SPH_PRECISION_FP32_COMPENSATED && p.dim == 2 ? 1 : 2);
+    // cells per r_cut; default 2: cells of r_cut/2 leave fewer candidates beyond r_cut
+    // (56 instead of 81 per particle in 2D, 422 instead of 729 in 3D), and a row of cells
+    // is walked as one contiguous run of the sorted arrays
+    const int m = p.cell_subdivision != 0 ? p.cell_subdivision : 2;
     if (m != 1 && m != 2) { err = "cell_subdivision must be 0, 1 or 2"; return false; }
     S.reach = m;
     // cell edge r_cut (1 + 1e-9) / m: a pair with d <= r_cut is at most m cells apart

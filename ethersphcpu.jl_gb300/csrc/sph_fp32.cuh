@@ -22,6 +22,8 @@
 // ThermalConduction.jl, SelfAction/*.jl and ReconstructValue.jl.
 #pragma once
 
+#include <climits>
+
 #include "sph_physics.cuh"
 #include "sph_kernels.h"
 
@@ -115,6 +117,35 @@ __device__ __forceinline__ float kernel_w_f(float q, const SceneDev& S) {
 // x-reach .. x+reach (wrapping on a periodic axis, skipped off the grid) form one virtual
 // range that the TPP lanes share.  The callback gets the sorted index j and the offset
 // of j's cell from i's cell in metres.
+// A neighbour row whose cells x-m .. x+m do not wrap is one contiguous run of the
+// sorted arrays, [b, e); the cell of a candidate follows from the interior cell
+// boundaries (at most 2m = 4 of them): dx = dx0 + #(boundaries <= j).
+struct RowRun {
+    int b, e, dx0;
+    int bnd[4];
+};
+
+__device__ __forceinline__ bool row_run(const SceneDev& S, const int32_t* __restrict__ start, int row, int cx,
+                                        RowRun& R) {
+    const int m = S.reach;
+    if (S.periodic_x && (cx - m < 0 || cx + m >= S.n[0])) return false;
+    const int x0 = cx - m < 0 ? 0 : cx - m;
+    const int x1 = cx + m >= S.n[0] ? S.n[0] - 1 : cx + m;
+    R.b = __ldg(start + row + x0);
+    R.e = __ldg(start + row + x1 + 1);
+    R.dx0 = x0 - cx;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int cell = x0 + 1 + q;
+        R.bnd[q] = cell <= x1 ? __ldg(start + row + cell) : INT_MAX;
+    }
+    return true;
+}
+
+__device__ __forceinline__ int run_dx(const RowRun& R, int j) {
+    return R.dx0 + (j >= R.bnd[0]) + (j >= R.bnd[1]) + (j >= R.bnd[2]) + (j >= R.bnd[3]);
+}
+
 template <int DIM, int TPP, typename F>
 __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
                                            int lane, F&& f) {
@@ -130,15 +161,16 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
             const float oy = (float)dy * S.cell_f[1];
             const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
             // the row's cells are one virtual range v = 0 .. (sum of lengths)-1; lane t
-            // takes v = t, t+TPP, ...  Each cell is walked in turn from the first v of
-            // the lane inside it (scalars only: every index stays in a register).
-            int prefix = 0;
+            // takes v = t, t+TPP, ...
+            RowRun R;
+            if (row_run(S, start, row, c[0], R)) {
+                for (int j = R.b + lane; j < R.e; j += TPP) f(j, (float)run_dx(R, j) * S.cell_f[0], oy, oz);
+                continue;
+            }
+            int prefix = 0;  // a wrapping row of a periodic axis: cell by cell
             for (int dx = -m; dx <= m; ++dx) {
                 int x = c[0] + dx;
-                bool ok = true;
-                if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
-                else ok = x >= 0 && x < S.n[0];
-                if (!ok) continue;
+                x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
                 const float ox = (float)dx * S.cell_f[0];
@@ -168,13 +200,27 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
             const float oy = (float)dy * S.cell_f[1];
             const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
-            int prefix = 0;
+            RowRun R;
+            if (row_run(S, start, row, c[0], R)) {
+                int j = R.b + lane;
+                if (j >= R.e) continue;
+                auto d = load(j);
+                for (;;) {
+                    const int jn = j + TPP;
+                    const bool more = jn < R.e;
+                    decltype(d) dn = d;
+                    if (more) dn = load(jn);
+                    f(j, d, (float)run_dx(R, j) * S.cell_f[0], oy, oz);
+                    if (!more) break;
+                    j = jn;
+                    d = dn;
+                }
+                continue;
+            }
+            int prefix = 0;  // a wrapping row of a periodic axis: cell by cell
             for (int dx = -m; dx <= m; ++dx) {
                 int x = c[0] + dx;
-                bool ok = true;
-                if (S.periodic_x) x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
-                else ok = x >= 0 && x < S.n[0];
-                if (!ok) continue;
+                x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
                 const float ox = (float)dx * S.cell_f[0];

@@ -1052,9 +1052,8 @@ bool load_model(const SphParams* p, Model* M, Kern* K) {
     M->check_interval = p->check_interval;
     M->check_enabled = p->check_enabled;
     M->periodic_x = p->periodic_x;
-    // the library's default: 1 for the FP32 form in 2D, else 2
-    M->cells_per_rc = p->cell_subdivision != 0 ? p->cell_subdivision
-                                               : (p->precision == SPH_PRECISION_FP32_COMPENSATED && p->dim == 2 ? 1 : 2);
+    // the library's default: 2 cells per r_cut
+    M->cells_per_rc = p->cell_subdivision != 0 ? p->cell_subdivision : 2;
     if (M->cells_per_rc != 1 && M->cells_per_rc != 2) return false;
     if (M->periodic_x) {
         const double edge = K->rc * (1.0 + 1e-9) / (double)M->cells_per_rc;
