@@ -38,7 +38,7 @@ MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of one momentum launch on the default workload, measured with
 # ncu --set full --clock-control none (cold L2, as the bench's flushed steps)
-MOMENTUM_DRAM_BYTES_256 = 7.610112e6
+MOMENTUM_DRAM_BYTES_256 = 7.897856e6
 
 
 def parse():
@@ -351,7 +351,7 @@ def run_ours(args, rank, world, local):
             "peak_source": f"{peak_src} hbm_gbs",
             "algorithmic_bytes_per_launch": bytes_mom,
             "traffic": MOMENTUM_DRAM_BYTES_256 if (args.n == 256 and args.precision == "fp32c") else None,
-            "traffic_source": "ncu --set full of this launch at n=256, shape -1,-1,-1,128: "
+            "traffic_source": "ncu --set full of this launch at n=256, shape -1,2,-1,128: "
                               "dram__bytes_read.sum + dram__bytes_write.sum",
             "note": ("FP64 pair arithmetic is ALU-bound on GB300 (FP64 at 1/64 of the FP32 rate)"
                      if args.precision == "fp64" else
