@@ -1526,7 +1526,17 @@ int32_t sph_output_write(SphHandle* h, int64_t file_step, double time) {
     src.start = h->sc.start;
     src.cell_lo = R.dev.cell_off;
     src.cell_hi = R.dev.cell_off + R.dev.ncells;
-    src.n_upper = std::min<int64_t>(h->n_upper, h->cap);
+    src.n_upper = h->has_buffers ? h->cap : std::min<int64_t>(h->n_upper, h->cap);  // inlet copies append
+    if (h->has_buffers) {
+        const BufferState& B = h->B[h->par];
+        src.bx = B.x;
+        src.bv = B.v;
+        const double* bf[5] = {B.rho, B.p, B.c, B.m, B.gap};
+        for (int k = 0; k < 5; ++k) src.bfield[k] = bf[k];
+        src.border = B.order;
+        src.bn = h->bn + h->par;
+        src.bcap = h->bcap;
+    }
     int rc = h->out->enqueue(h->stream, src, file_step, time, err);
     if (rc != SPH_OK) return fail(h, rc, err);
     return SPH_OK;

@@ -7,7 +7,8 @@
 //   field data  Step (Int64), Time (Float64), WallTime ("yyyy/mm/dd__HH:MM:SS.SS",
 //               DataIO.jl:10, in which Julia's Dates reads "SS" as the second both times)
 //   point data  Velocity (dim components; NaN for groups without a velocity, :72-80),
-//               Type (Int64: 1 for the fluid, 2, 3, ... for the wall groups, :67-69),
+//               Type (Int64: 1 for the fluid, then the inlet and outlet particles of
+//               the inlet/outlet solve, then the wall groups: 2, 3, ..., :67-69),
 //               one Float64 column per field symbol (NaN where the group's particle
 //               type has no such field, getParticleFields! :21-38)
 //   points      3 components (z = 0 in 2D); one vertex per particle.
@@ -32,6 +33,8 @@ namespace sph {
 namespace {
 
 constexpr size_t kAlign = 256;
+// order key of an outlet particle (the library's buffer order: bit 62 = outlet)
+constexpr int64_t kOutletOrderBit = int64_t(1) << 62;
 size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 int cuda_err(cudaError_t e, const char* what, std::string& err) {
@@ -270,6 +273,33 @@ int VtpWriter::enqueue(cudaStream_t compute, const FluidSnapshotSrc& src, int64_
         j.off_field[c] = off;
         off += align_up(n * 8);
     }
+    const size_t nb = src.bx ? (size_t)std::max<int64_t>(src.bcap, 0) : 0;
+    j.buffers = src.bx != nullptr;
+    j.bcap = (int64_t)nb;
+    if (src.bx) {  // inlet/outlet buffers: all fields, the order keys, the live count
+        j.off_bx = off;
+        off += align_up(nb * vb);
+        j.off_bv = off;
+        off += align_up(nb * vb);
+        for (int f = 0; f < 5; ++f) {
+            j.off_bfield[f] = off;
+            off += align_up(nb * 8);
+        }
+        j.off_border = off;
+        off += align_up(nb * 8);
+        j.off_bn = off;
+        off += kAlign;
+    }
+    if (off > s.bytes) {  // a larger state than the slot was sized for: grow it (it is idle)
+        if (s.dbuf) cudaFree(s.dbuf);
+        if (s.hbuf) cudaFreeHost(s.hbuf);
+        s.dbuf = nullptr;
+        s.hbuf = nullptr;
+        s.bytes = 0;
+        OUT_CUDA(cudaMalloc(&s.dbuf, off), "output staging (device)");
+        OUT_CUDA(cudaMallocHost(&s.hbuf, off), "output staging (pinned host)");
+        s.bytes = off;
+    }
     // device-to-device copies, ordered after the steps on the step stream
     if (n > 0) {
         OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_x, src.x, n * vb, cudaMemcpyDeviceToDevice, compute), "stage x");
@@ -285,6 +315,19 @@ int VtpWriter::enqueue(cudaStream_t compute, const FluidSnapshotSrc& src, int64_
              "stage range");
     OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_range + 4, src.start + src.cell_hi, 4, cudaMemcpyDeviceToDevice, compute),
              "stage range");
+    if (src.bx) {
+        if (nb > 0) {
+            OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_bx, src.bx, nb * vb, cudaMemcpyDeviceToDevice, compute), "stage");
+            OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_bv, src.bv, nb * vb, cudaMemcpyDeviceToDevice, compute), "stage");
+            for (int f = 0; f < 5; ++f)
+                OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_bfield[f], src.bfield[f], nb * 8, cudaMemcpyDeviceToDevice,
+                                         compute),
+                         "stage");
+            OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_border, src.border, nb * 8, cudaMemcpyDeviceToDevice, compute),
+                     "stage");
+        }
+        OUT_CUDA(cudaMemcpyAsync(s.dbuf + j.off_bn, src.bn, 4, cudaMemcpyDeviceToDevice, compute), "stage");
+    }
     OUT_CUDA(cudaEventRecord(s.staged, compute), "output event record");
     // the copy stream takes it from there
     OUT_CUDA(cudaStreamWaitEvent(copy_, s.staged, 0), "output stream wait");
@@ -371,9 +414,31 @@ int VtpWriter::write_file(const Job& j, std::string& err) {
     for (int32_t q = 0; q <= max_id; ++q)
         if (at[(size_t)q] >= 0) order.push_back(at[(size_t)q]);
 
+    // inlet and outlet particles (sorted by order key within each group)
+    std::vector<int64_t> inl, outl;
+    const double* bx = nullptr;
+    const double* bv = nullptr;
+    const int64_t* bo = nullptr;
+    if (j.buffers) {
+        int32_t nb = 0;
+        std::memcpy(&nb, hb + j.off_bn, 4);
+        if (nb < 0 || nb > j.bcap) {
+            err = "output: buffer count outside the staged particles";
+            return SPH_ERR_STATE;
+        }
+        bx = (const double*)(hb + j.off_bx);
+        bv = (const double*)(hb + j.off_bv);
+        bo = (const int64_t*)(hb + j.off_border);
+        for (int64_t k = 0; k < nb; ++k) (bo[k] & kOutletOrderBit ? outl : inl).push_back(k);
+        auto by_order = [&](int64_t a, int64_t c) { return bo[a] < bo[c]; };
+        std::sort(inl.begin(), inl.end(), by_order);
+        std::sort(outl.begin(), outl.end(), by_order);
+    }
+    const int64_t nbuf = (int64_t)(inl.size() + outl.size());
+
     int64_t nw = 0;
     for (const WallGroupHost& g : walls_) nw += g.n;
-    const int64_t n = nf + nw;
+    const int64_t n = nf + nbuf + nw;
     const double nan = std::numeric_limits<double>::quiet_NaN();
 
     std::vector<double> vel((size_t)n * dim), pts((size_t)n * 3, 0.0);
@@ -397,6 +462,27 @@ int VtpWriter::write_file(const Job& j, std::string& err) {
     }
     int64_t o = nf;
     int64_t group = 2;
+    if (bx) {  // the inlet group, then the outlet group: CommonLiquidParticle vectors
+        const std::vector<int64_t>* parts[2] = {&inl, &outl};
+        for (const std::vector<int64_t>* part : parts) {
+            for (size_t q = 0; q < part->size(); ++q) {
+                const size_t k = (size_t)(*part)[q];
+                for (int a = 0; a < dim; ++a) {
+                    pts[(size_t)(o + q) * 3 + a] = bx[k * stride + a];
+                    vel[(size_t)(o + q) * dim + a] = bv[k * stride + a];
+                }
+                type[(size_t)(o + q)] = group;
+            }
+            for (size_t c = 0; c < col_fluid_.size(); ++c) {
+                const int f = col_fluid_[c];  // rho_ p_ c_ mass_ gap_ exist; thermal fields do not
+                const double* src = f >= 0 && f < 5 ? (const double*)(hb + j.off_bfield[f]) : nullptr;
+                for (size_t q = 0; q < part->size(); ++q)
+                    cols[c][(size_t)(o + q)] = src ? src[(*part)[q]] : nan;
+            }
+            o += (int64_t)part->size();
+            ++group;
+        }
+    }
     for (const WallGroupHost& g : walls_) {
         const bool has_v = g.kind == SPH_WALL_STATIC_VELOCITY;
         for (int64_t i = 0; i < g.n; ++i) {

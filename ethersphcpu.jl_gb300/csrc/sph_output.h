@@ -36,6 +36,15 @@ struct FluidSnapshotSrc {
     const int32_t* start;
     int32_t cell_lo, cell_hi;
     int64_t n_upper;
+    // inlet/outlet buffer particles (null bx: none): sorted arrays, live count, capacity;
+    // written as the inlet group and the outlet group between the fluid and the walls
+    // (FluidInletOutletWallSolve.jl:282), each in ascending order key
+    const void* bx;
+    const void* bv;
+    const double* bfield[5];  // rho p c mass gap
+    const int64_t* border;
+    const int32_t* bn;
+    int64_t bcap;
 };
 
 // One wall group (one sph_upload_walls call), host arrays in upload order.
@@ -81,6 +90,9 @@ private:
         double time;
         size_t off_x, off_v, off_id, off_range, off_field[FF_COUNT];
         int64_t n_upper;
+        bool buffers;  // the file holds the inlet and outlet groups
+        size_t off_bx, off_bv, off_bfield[5], off_border, off_bn;
+        int64_t bcap;
     };
     void worker();
     int write_file(const Job& job, std::string& err);

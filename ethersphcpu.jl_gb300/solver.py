@@ -337,7 +337,7 @@ def solve_inlet_outlet(fluid, inlet, outlet, walls, kernel, model, td, vtp_io=No
                        user_defined_function=None, udf_interval: int = 1, precision: int = _abi.PRECISION_FP64,
                        domain_lo=None, domain_hi=None, first_step: int = 1, nsteps: int | None = None,
                        fluid_capacity: int | None = None, buffer_capacity: int | None = None,
-                       wall_time: str | None = None):
+                       staged_output: bool = True, wall_time: str | None = None):
     """GPU counterpart of the inlet/outlet solve!(fluid, inlet, outlet, walls, kernel,
     model, td, vtp_io; checks..., user_defined_function) (FluidInletOutletWallSolve.jl:
     264-340).  rules: InletOutletRules (the check/modify closures as planes).
@@ -359,6 +359,9 @@ def solve_inlet_outlet(fluid, inlet, outlet, walls, kernel, model, td, vtp_io=No
     def write(step_file, t):
         if vtp_io is None:
             return
+        if staged_output:  # the library copies the state and writes the file meanwhile
+            sim.output_write(step_file, t)
+            return
         _buffers_into(sim, inlet, 0)
         _buffers_into(sim, outlet, 1)
         _fluid_into(sim, fluid)
@@ -368,6 +371,8 @@ def solve_inlet_outlet(fluid, inlet, outlet, walls, kernel, model, td, vtp_io=No
         sim.upload_walls(walls)
         sim.upload_fluid(fluid)
         sim.upload_buffers(rules, inlet, outlet, buffer_capacity)
+        if vtp_io is not None and staged_output:
+            sim.output_open(vtp_io, wall_time)
         write(0, 0.0)
         step = first_step
         while step <= last:
@@ -381,6 +386,8 @@ def solve_inlet_outlet(fluid, inlet, outlet, walls, kernel, model, td, vtp_io=No
                 user_defined_function(sim, nxt * td.dt_)
             if vtp_io is not None and isOutputStep(nxt, td):
                 write(nxt // td.output_interval_, nxt * td.dt_)
+        if vtp_io is not None and staged_output:
+            sim.output_flush()
         _fluid_into(sim, fluid)
         _buffers_into(sim, inlet, 0)
         _buffers_into(sim, outlet, 1)

@@ -399,8 +399,9 @@ int32_t sph_probe(SphHandle* h, int64_t n_points, const double* points, int32_t 
  * ignored); a symbol a group's particle type lacks gives NaN for that group, as
  * getParticleFields! (VTPIO.jl:21-38); vector and accumulator fields (x_vec_, drho_, ...)
  * are SPH_ERR_ARG.  wall_time: fixed WallTime text for every file, or NULL for the
- * clock.  Groups: the fluid (Type 1), then each sph_upload_walls call in call order
- * (Type 2, 3, ...).  Files use the VTK XML appended raw layout with UInt64 headers. */
+ * clock.  Groups: the fluid (Type 1), then, for the inlet/outlet solve, the inlet and
+ * the outlet particles (FluidInletOutletWallSolve.jl:282), then each sph_upload_walls
+ * call in call order.  Files use the VTK XML appended raw layout with UInt64 headers. */
 int32_t sph_output_open(SphHandle* h, const char* dir_path, const char* file_name, const char* file_suffix,
                         int32_t step_digit, int32_t n_fields, const char* const* field_symbols,
                         const char* const* field_names, const char* wall_time);

@@ -219,3 +219,29 @@ def test_inlet_outlet_channel_follows_the_transient_profile(pkg, tmp_path):
     last = vtp.read_vtp_arrays(str(tmp_path / "channel_15.vtp"))
     assert set(np.unique(last["Type"])) == {1, 2, 3, 4}        # fluid, inlet, outlet, walls
     assert int(np.sum(last["Type"] == 1)) == len(fluid)
+
+
+@pytest.mark.gpu
+def test_inlet_outlet_staged_files_equal_host_writer(pkg, tmp_path):
+    # the library's staged writer puts the inlet and outlet groups between the fluid and
+    # the walls exactly as the host writer does (writeVTP's [fluid, inlet, outlet, walls])
+    import filecmp
+    import os
+    from ethersph_gb300 import scenes, vtp
+    files = {}
+    for staged in (True, False):
+        s = scenes.poiseuille_inlet_outlet_2d(n_across=10, total_step=240)
+        m = s.meta
+        d = tmp_path / ("staged" if staged else "host")
+        io = vtp.VTPIO(3, "io_", ".vtp", str(d), ["rho_", "p_", "mass_", "t_"], ["Density", "Pressure", "Mass", "T"])
+        pkg.solve_inlet_outlet(s.fluid, m["inlet"], m["outlet"], s.walls[0], s.kernel, s.model, s.td, io,
+                               rules=m["rules"], domain_lo=s.domain_lo, domain_hi=s.domain_hi,
+                               staged_output=staged, wall_time="2026/12/03__01:02:03.03")
+        files[staged] = d
+    names = sorted(os.listdir(files[False]))
+    assert names == sorted(os.listdir(files[True])) and len(names) == 3
+    for f in names:
+        assert filecmp.cmp(files[True] / f, files[False] / f, shallow=False), f
+    last = vtp.read_vtp_arrays(str(files[True] / names[-1]))
+    assert set(np.unique(last["Type"])) == {1, 2, 3, 4}
+    assert np.all(np.isnan(last["T"]))
