@@ -36,9 +36,14 @@ sys.path.insert(0, str(ROOT))
 METRIC = "particle-steps/s"
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of one momentum launch on the default workload, measured with
-# ncu --set full --clock-control none (cold L2, as the bench's flushed steps)
-MOMENTUM_DRAM_BYTES_256 = 7.897856e6
+LANES_LIST = 16  # SPH_LANES_LIST: momentum lanes codes >= 15 read the neighbour list
+# DRAM bytes (read + write) of one launch of each gather on the default workload (n=256,
+# FP32-compensated), measured with ncu --set full --clock-control none (cold L2, as the
+# bench's flushed steps), with the launch shape they were captured at
+DRAM_BYTES_256 = {
+    "continuity": (None, None),
+    "momentum": (7.897856e6, "-1,2,-1,128"),
+}
 
 
 def parse():
@@ -173,20 +178,34 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- our arm
-def algorithmic_bytes(scene, precision):
-    """Bytes the momentum kernel must move for one launch on the 2D thermal cavity (each
-    per-particle SoA element it reads or writes, once; neighbour re-reads count zero):
-    the numerator of roofline.achieved."""
+def algorithmic_bytes(scene, precision, stage, list_entries=0.0):
+    """Bytes one launch of the continuity (K4) or momentum (K5) gather must move on the 2D
+    thermal cavity: each per-particle SoA element the kernel reads or writes, once
+    (neighbour re-reads count zero; the neighbour list, when the launch shape uses it, is
+    a per-particle array of `list_entries` 4-byte entries on average plus a 4-byte count,
+    written once by K4 and read once by K5).  The numerator of roofline.achieved."""
     nf, nw = scene.n_fluid, scene.n_wall
     assert scene.fluid.x_vec_.shape[1] == 2 and scene.fluid.thermal
+    lst = 4 + 4 * list_entries if list_entries else 0
+    if stage == "continuity":
+        if precision == "fp64":
+            fluid = (16 + 16 + 8 + 8 + 4) + 4 * 8    # x v m rho scene | rhoc p c P
+        else:
+            fluid = (16 + 16 + 4 + 4 + 8 + 8) + (5 * 8 + 16) + lst  # fa fb cell scene rho m | rhoc p c P vol fb
+        return nf * fluid
     writes = 16 + 16 + 8 + 8 + 4 + 4  # x' v' (double2) T' rho' key slot
     if precision == "fp64":
         fluid = (16 + 16 + 8 * 8 + 4) + writes  # x v | rhoc P m gap c T kappa cp | scene
         wall = 16 + 16 + 16 + 8 + 8 + 8 + 4     # x n v gap T kappa kind
     else:
-        fluid = (16 + 16 + 16 + 8 + 4 + 4 + 16 + 16 + 8 + 8) + writes  # fa fb fc c cell scene | x v T rhoc
-        wall = 16 + 16 + 16                                           # float4 shadows fa fb fc
+        fluid = (16 + 16 + 16 + 8 + 4 + 4 + 16 + 16 + 8 + 8) + writes + lst  # fa fb fc c cell scene | x v T rhoc
+        wall = 16 + 16 + 16                                                 # float4 shadows fa fb fc
     return nf * fluid + nw * wall
+
+
+def scan_launches(cells):
+    """Kernels of one cell scan (sph_sort.cu launch_scan)."""
+    return 1 if cells <= 16384 else (2 if cells <= 64 * 4096 else 3)
 
 
 def grid_cells(scene, precision):
@@ -284,16 +303,44 @@ def run_ours(args, rank, world, local):
     value = scene.n_fluid * args.steps * world / (ms_max / 1e3)
     clocks = clk.summary()
 
-    # per-stage times (CUDA events on the handle's stream), dominant kernel roofline
+    # per-stage times (CUDA events on the handle's stream), roofline of the two gathers
     stages = sim.time_stages(20)
-    mom_ms = stages["momentum"]
-    bytes_mom = algorithmic_bytes(scene, args.precision)
     peaks = json.loads(MEASURED_PEAKS.read_text()) if MEASURED_PEAKS.exists() else {}
     hbm = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or FALLBACK_HBM_GBS
-    achieved = bytes_mom / (mom_ms / 1e3) / 1e9
     pairs_ff, pairs_fw = sim.count_pairs()
+    uses_list = args.precision == "fp32c" and launch_shape[1] >= LANES_LIST - 1
+    entries = 2.0 * pairs_ff / scene.n_fluid if uses_list else 0.0
+    shape_txt = ",".join(str(v) for v in launch_shape)
+
+    def roofline(stage, label):
+        b = algorithmic_bytes(scene, args.precision, stage, entries)
+        achieved = b / (stages[stage] / 1e3) / 1e9
+        traffic, at = DRAM_BYTES_256[stage] if (args.n == 256 and args.precision == "fp32c") else (None, None)
+        return {
+            "bound": "hbm",
+            "kernel": label,
+            "achieved": achieved,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": achieved / hbm,
+            "peak_source": f"{peak_src} hbm_gbs",
+            "algorithmic_bytes_per_launch": b,
+            "neighbour_list_bytes_per_launch": (4 + 4 * entries) * scene.n_fluid if uses_list else 0,
+            "launch_ms": stages[stage],
+            "traffic": traffic,
+            "traffic_source": (f"ncu --set full of this launch at n=256, shape {at}: "
+                               "dram__bytes_read.sum + dram__bytes_write.sum" if traffic else None),
+            "traffic_shape_matches": (at == shape_txt) if traffic else None,
+            "note": ("FP64 pair arithmetic is ALU-bound on GB300 (FP64 at 1/64 of the FP32 rate)"
+                     if args.precision == "fp64" else
+                     "issue/latency-bound: dependent neighbour loads and pair arithmetic, not bytes"),
+        }
+
+    roof = {"continuity": roofline("continuity", "continuity + EOS (K4)"),
+            "momentum": roofline("momentum", "momentum + integrate, the fused pair kernel (K5)")}
+    dominant = max(roof, key=lambda k: stages[k])
 
     # e2e through the C ABI with host buffers: upload, 100 steps, download
     r = {}
@@ -341,31 +388,17 @@ def run_ours(args, rank, world, local):
         "pair_interactions_per_s": pairs_ff * args.steps * world / (ms_max / 1e3),
         "pairs": {"fluid_fluid_unique": pairs_ff, "fluid_wall": pairs_fw},
         "stages_ms": stages,
-        "roofline": {
-            "bound": "hbm",
-            "kernel": "momentum (K5)",
-            "achieved": achieved,
-            "peak": hbm,
-            "unit": "GB/s",
-            "frac": achieved / hbm,
-            "peak_source": f"{peak_src} hbm_gbs",
-            "algorithmic_bytes_per_launch": bytes_mom,
-            "traffic": MOMENTUM_DRAM_BYTES_256 if (args.n == 256 and args.precision == "fp32c") else None,
-            "traffic_source": "ncu --set full of this launch at n=256, shape -1,2,-1,128: "
-                              "dram__bytes_read.sum + dram__bytes_write.sum",
-            "note": ("FP64 pair arithmetic is ALU-bound on GB300 (FP64 at 1/64 of the FP32 rate)"
-                     if args.precision == "fp64" else
-                     "issue/latency-bound: dependent neighbour loads and pair arithmetic, not bytes"),
-        },
+        "roofline": roof[dominant],
+        "roofline_other_gather": roof["continuity" if dominant == "momentum" else "momentum"],
         "e2e": {"value": e2e_val, "unit": METRIC, "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
                 "what": f"upload + {e2e_steps} steps + download per iteration, {e2e_iters} iterations"},
         "plain_fp64": other,
         "launch_shape": {"continuity_lanes": launch_shape[0], "momentum_lanes": launch_shape[1],
                          "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": chosen_by},
-        # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, else 3), fill,
-        # placement; plus the Shepard kernel on re-initialisation steps
-        "gpu_launches": args.steps * (4 + (1 if grid_cells(scene, prec) <= 16384 else 3)) + reinit_steps,
+        # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, 2 up to
+        # 262,144, else 3), fill, placement; plus the Shepard kernel on re-initialisation steps
+        "gpu_launches": args.steps * (4 + scan_launches(grid_cells(scene, prec))) + reinit_steps,
         "clocks": clocks,
     }
     return out

@@ -165,6 +165,7 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.nan_check = p.nan_check;
     S.dt = p.dt;
     S.dtdt = p.dt * p.dt;
+    S.half_dtdt = S.dtdt * 0.5;
     S.reinit_interval = p.density_reinitialized_interval;
     S.check_interval = p.check_interval;
 
@@ -180,6 +181,7 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.c0_f = (float)p.c_0;
     S.rho0_f = (float)p.rho_0;
     S.inv_cp_f = (float)S.inv_cp_d;
+    S.inv_rho0 = 1.0 / p.rho_0;
     S.inv_rho0_f = (float)(1.0 / p.rho_0);
     return true;
 }
@@ -222,6 +224,7 @@ struct SceneRec {
     std::vector<int64_t> wgroup_end;  // end of each sph_upload_walls group in the host copy
     double gap0 = 0.0;                // gap of the first uploaded fluid particle
     bool uniform_fluid = true;        // every uploaded fluid particle has gap0
+    int32_t list_depth = 0;           // neighbour-list entries per particle this scene asks for
 };
 
 // First-fit allocator of ranges in [0, cap).
@@ -298,6 +301,9 @@ struct SphHandle {
     int64_t steps_done = 0;
     // FP32 launch shape: lanes per particle for continuity, momentum, Shepard; block size
     int tune[4] = {1, 1, 1, 128};  // the autotuner's most frequent pick on large 2D and 3D scenes
+    // neighbour list of the FP32 form (momentum lanes code >= SPH_LANES_LIST - 1): grown
+    // on demand to the per-particle grid and the deepest scene (ensure_list)
+    NbrList nl{};
     std::string err;
     std::vector<SceneRec> scenes;
     RangeAlloc cells, walls;
@@ -389,6 +395,65 @@ cudaError_t alloc_sorted(SphHandle* h, SortedState& s) {
     return cudaSuccess;
 }
 
+// Rows of the per-particle grids: the live bound, not the capacity (a served batch is
+// sized for its memory budget and may hold far fewer particles); with inlet/outlet
+// buffers the capacity, since fluid particles made from the inlet are appended behind
+// the live ones.
+int32_t grid_rows(const SphHandle* h) {
+    if (h->has_buffers) return (int32_t)h->cap;
+    return (int32_t)std::max<int64_t>(1, std::min<int64_t>(h->cap, h->n_upper));
+}
+
+bool uses_list(const SphHandle* h) {
+    return h->precision == SPH_PRECISION_FP32_COMPENSATED && h->tune[1] >= SPH_LANES_LIST - 1;
+}
+
+// Neighbour-list entries a particle of spacing `gap` needs: the lattice points within
+// r_cut of a lattice point, with a quarter of headroom for compression (a particle with
+// more neighbours walks the cells instead).
+int32_t list_depth_for(int dim, double rc2, double gap) {
+    if (!(gap > 0.0) || !(rc2 > 0.0)) return 64;
+    const double R2 = rc2 / (gap * gap) * (1.0 + 1e-9);
+    const int R = (int)std::min(16.0, std::floor(std::sqrt(R2)));
+    int64_t count = 0;
+    for (int a = -R; a <= R; ++a)
+        for (int b = -R; b <= R; ++b)
+            for (int c = (dim == 3 ? -R : 0); c <= (dim == 3 ? R : 0); ++c)
+                count += (double)(a * a + b * b + c * c) <= R2;
+    const int64_t depth = ((int64_t)std::ceil(1.25 * (double)(count - 1)) + 8 + 7) / 8 * 8;
+    return (int32_t)std::min<int64_t>(depth, 1024);
+}
+
+// Storage of the neighbour list for the current per-particle grid and scene depths;
+// reallocating drops the captured graphs (they hold its address).
+int32_t ensure_list(SphHandle* h) {
+    if (!uses_list(h)) return SPH_OK;
+    int32_t depth = 8;
+    for (const SceneRec& R : h->scenes)
+        if (R.used) depth = std::max(depth, R.list_depth);
+    const int64_t rows = grid_rows(h);
+    if (h->nl.e && rows <= h->nl.stride && depth <= h->nl.kmax) return SPH_OK;
+    SPH_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->nl.e) cudaFree(h->nl.e);
+    if (h->nl.n) cudaFree(h->nl.n);
+    h->nl = NbrList{};
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+    const int64_t stride = std::max<int64_t>(rows, 1);
+    cudaError_t e = cudaMalloc((void**)&h->nl.e, (size_t)stride * (size_t)depth * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->nl.n, (size_t)stride * 4);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (h->nl.e) cudaFree(h->nl.e);
+        h->nl = NbrList{};
+        return fail(h, SPH_ERR_OOM, "no device memory for the neighbour list (" + std::to_string(stride) + " x " +
+                                        std::to_string(depth) + " entries); use a cell-walk momentum lanes code");
+    }
+    h->nl.kmax = depth;
+    h->nl.stride = stride;
+    return SPH_OK;
+}
+
 LaunchCtx make_ctx(SphHandle* h) {
     LaunchCtx L{};
     L.stream = h->stream;
@@ -397,9 +462,7 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.mode = h->mode;
     L.thermal = h->thermal;
     L.precision = h->precision;
-    // per-particle grids cover the live bound, not the capacity (a served batch is sized
-    // for its memory budget and may hold far fewer particles)
-    L.cap = (int32_t)std::max<int64_t>(1, std::min<int64_t>(h->cap, h->n_upper));
+    L.cap = grid_rows(h);
     L.total_cells = h->scan_cells;
     L.nscenes = h->scap;
     L.scenes = h->d_scenes;
@@ -415,10 +478,10 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.tpp_continuity = h->tune[0];
     L.tpp_momentum = h->tune[1];
     L.tpp_reinit = h->tune[2];
+    L.list_momentum = uses_list(h);
+    if (L.list_momentum) L.tpp_momentum -= SPH_LANES_LIST;
+    L.nl = h->nl;
     if (h->has_buffers) {
-        // fluid particles made from the inlet are appended behind the live ones: the
-        // per-particle grids cover the capacity
-        L.cap = (int32_t)h->cap;
         L.bf = h->B[h->par];
         L.bf.n = h->bn + h->par;
         L.bf.start = h->bs.start;
@@ -665,6 +728,9 @@ int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const dou
             hc[i] = S.c0 * std::sqrt(host_powi(rr, S.gamma - 1));
         }
     }
+    double gmin = 0.0;
+    for (int64_t i = 0; i < n; ++i) gmin = (i == 0 || gap[i] < gmin) ? gap[i] : gmin;
+    h->scenes[s].list_depth = n > 0 ? list_depth_for(dim, S.rc2, gmin) : 0;
     std::vector<int32_t> ids(n), scn(n, s);
     for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
     SortedState& d = h->S[h->par];
@@ -750,6 +816,7 @@ int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, do
 // Run nsteps steps of every scene (each at its own step number) as CUDA-graph bundles.
 int32_t step_all_async(SphHandle* h, int64_t nsteps) {
     cudaStream_t st = h->stream;
+    if (int32_t rc = ensure_list(h); rc != SPH_OK) return rc;
     const int64_t bundle = 10;
     int64_t done = 0;
     while (done < nsteps) {
@@ -1336,6 +1403,7 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
     if (!h || !ms_out || reps < 1) return fail(h, SPH_ERR_ARG, "bad argument");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
     cudaStream_t st = h->stream;
+    if (int32_t rc = ensure_list(h); rc != SPH_OK) return rc;
     cudaEvent_t e0, e1;
     SPH_CUDA(h, cudaEventCreate(&e0));
     SPH_CUDA(h, cudaEventCreate(&e1));
@@ -1394,6 +1462,13 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
     if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
         cudaStream_t st = h->stream;
+        // storage for the list candidates (kept only when a list shape wins; released
+        // with the handle)
+        const int saved1 = h->tune[1];
+        h->tune[1] = SPH_LANES_LIST + 1;
+        const bool have_list = ensure_list(h) == SPH_OK;
+        h->tune[1] = saved1;
+        if (!have_list) h->err.clear();
         cudaEvent_t e0, e1;
         SPH_CUDA(h, cudaEventCreate(&e0));
         SPH_CUDA(h, cudaEventCreate(&e1));
@@ -1403,38 +1478,90 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         // overwrite them, so park them in the idle sorted buffer meanwhile
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].p, h->S[par].p, nbytes, cudaMemcpyDeviceToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(h->S[par ^ 1].c, h->S[par].c, nbytes, cudaMemcpyDeviceToDevice, st));
-        const int tpps[5] = {-1, 1, 2, 4, 8};  // -1: one lane, software-pipelined loop
         const int blocks[3] = {64, 128, 256};
-        int best_tpp[3] = {4, 4, 4};
-        int best_block[3] = {128, 128, 128};
-        for (int stage = 0; stage < 3; ++stage) {
-            float best = 1e30f;
-            for (int tpp : tpps)
+        // time `reps` launches of one stage at one shape; list: continuity records the
+        // neighbour list / momentum reads it
+        auto trial = [&](int stage, int tpp, int block, bool list) -> float {
+            LaunchCtx L = make_ctx(h);
+            L.force_reinit = 1;
+            L.bs.npend = nullptr;  // trial launches mark no particle for the outlet
+            L.block = block;
+            L.tpp_continuity = L.tpp_momentum = L.tpp_reinit = tpp;
+            L.list_momentum = list ? 1 : 0;
+            L.nl = h->nl;
+            launch_physics(stage, L);  // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps; ++r) launch_physics(stage, L);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            return ms;
+        };
+        struct Best {
+            float ms = 1e30f;
+            int tpp = 1, block = 128;
+        };
+        auto search = [&](int stage, const int* tpps, int ntpp, bool list) {
+            Best b;
+            for (int q = 0; q < ntpp; ++q)
                 for (int block : blocks) {
-                    LaunchCtx L = make_ctx(h);
-                    L.force_reinit = 1;
-                    L.bs.npend = nullptr;  // trial launches mark no particle for the outlet
-                    L.block = block;
-                    L.tpp_continuity = L.tpp_momentum = L.tpp_reinit = tpp;
-                    launch_physics(stage, L);  // warm-up
-                    SPH_CUDA(h, cudaEventRecord(e0, st));
-                    for (int r = 0; r < reps; ++r) launch_physics(stage, L);
-                    SPH_CUDA(h, cudaEventRecord(e1, st));
-                    SPH_CUDA(h, cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    SPH_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
-                    if (ms < best) {
-                        best = ms;
-                        best_tpp[stage] = tpp;
-                        best_block[stage] = block;
-                    }
+                    if (tpps[q] == -1 && stage == 1 && block > 256) continue;
+                    const float ms = trial(stage, tpps[q], block, list);
+                    if (ms < b.ms) b = Best{ms, tpps[q], block};
                 }
+            return b;
+        };
+        const int walk_tpps[5] = {-1, 1, 2, 4, 8};  // -1: one lane, software-pipelined loop
+        const Best c_walk = search(0, walk_tpps, 5, false);
+        const Best m_walk = search(1, walk_tpps, 5, false);
+        const Best r_walk = search(2, walk_tpps, 5, false);
+        Best c_list, m_list;
+        if (have_list) {
+            const int c_tpps[2] = {-1, 1}, m_tpps[4] = {-1, 1, 2, 4};
+            c_list = search(0, c_tpps, 2, true);
+            // the momentum trials read the list the last continuity trial recorded
+            trial(0, c_list.tpp, c_list.block, true);
+            m_list = search(1, m_tpps, 4, true);
         }
+        // the cell-walk pair against the list pair, each timed as it runs in a step
+        // (continuity then momentum, at the momentum stage's block size)
+        auto pair_ms = [&](const Best& c, const Best& m, bool list) -> float {
+            LaunchCtx L = make_ctx(h);
+            L.force_reinit = 1;
+            L.bs.npend = nullptr;
+            L.block = m.block;
+            L.tpp_continuity = c.tpp;
+            L.tpp_momentum = m.tpp;
+            L.list_momentum = list ? 1 : 0;
+            L.nl = h->nl;
+            launch_physics(0, L);
+            launch_physics(1, L);
+            const int n = std::max(reps, 5);
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < n; ++r) {
+                launch_physics(0, L);
+                launch_physics(1, L);
+            }
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            return ms;
+        };
+        const bool pick_list = have_list && pair_ms(c_list, m_list, true) < pair_ms(c_walk, m_walk, false);
+        SPH_CUDA(h, cudaGetLastError());
         // one block size for all three stages: the momentum stage's (it dominates)
-        h->tune[0] = best_tpp[0];
-        h->tune[1] = best_tpp[1];
-        h->tune[2] = best_tpp[2];
-        h->tune[3] = best_block[1];
+        if (pick_list) {
+            h->tune[0] = c_list.tpp;
+            h->tune[1] = SPH_LANES_LIST + m_list.tpp;
+            h->tune[3] = m_list.block;
+        } else {
+            h->tune[0] = c_walk.tpp;
+            h->tune[1] = m_walk.tpp;
+            h->tune[3] = m_walk.block;
+        }
+        h->tune[2] = r_walk.tpp;
         // restore what the timed launches touched: p and c, and the arrivals left in
         // count[]; every other field they wrote is rebuilt by the next step before use
         SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
@@ -1455,12 +1582,22 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
 
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
     if (!h || !shape) return fail(h, SPH_ERR_ARG, "null argument");
-    for (int k = 0; k < 3; ++k)
-        if (shape[k] != -1 && shape[k] != 1 && shape[k] != 2 && shape[k] != 4 && shape[k] != 8)
-            return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
+    auto walk_code = [](int v) { return v == -1 || v == 1 || v == 2 || v == 4 || v == 8; };
+    const bool list = shape[1] >= SPH_LANES_LIST - 1;
+    if (!walk_code(shape[0]) || !walk_code(shape[2]))
+        return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
+    if (list) {
+        const int t = shape[1] - SPH_LANES_LIST;
+        if (t != -1 && t != 1 && t != 2 && t != 4)
+            return fail(h, SPH_ERR_ARG, "neighbour-list momentum lanes must be SPH_LANES_LIST + 1, 2, 4 or -1");
+        if (shape[0] != 1 && shape[0] != -1)
+            return fail(h, SPH_ERR_ARG, "the neighbour list is recorded by one continuity lane (1 or -1)");
+    } else if (!walk_code(shape[1])) {
+        return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
+    }
     if (shape[3] < 32 || shape[3] > 1024 || shape[3] % 32 != 0)
         return fail(h, SPH_ERR_ARG, "block size must be a multiple of 32 in [32, 1024]");
-    if (shape[1] == -1 && shape[3] > 256)
+    if ((shape[1] == -1 || shape[1] == SPH_LANES_LIST - 1) && shape[3] > 256)
         return fail(h, SPH_ERR_ARG, "the pipelined momentum walk (-1) takes blocks of at most 256 threads");
     for (int k = 0; k < 4; ++k) h->tune[k] = shape[k];
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
@@ -1767,6 +1904,8 @@ int32_t sph_destroy(SphHandle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     for (void* p : h->allocs) cudaFree(p);
+    if (h->nl.e) cudaFree(h->nl.e);
+    if (h->nl.n) cudaFree(h->nl.n);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;

@@ -59,7 +59,7 @@ struct SceneDev {
     int32_t uniform_gap;
     int32_t check_enabled;
     int32_t nan_check;
-    double dt, dt2half_unused;
+    double dt, half_dtdt;  // half_dtdt = dt * dt * 0.5 (scaling by 0.5 is exact)
     double dtdt;     // dt * dt
     int64_t reinit_interval;
     int64_t check_interval;
@@ -68,7 +68,7 @@ struct SceneDev {
     int32_t pad_active;
     double check_lo[3];
     double check_hi[3];
-    double two_pi_unused;
+    double inv_rho0;  // 1 / rho0 (FP32-compensated form's equation of state)
 
     // FP32-compensated form
     float cell_f[3];   // cell edge per axis (float)
@@ -136,6 +136,23 @@ struct WallState {
     int32_t* cell;
     int64_t n;
 };
+
+// Neighbour list of the FP32 form: the continuity gather records, in its walk order,
+// every neighbour within r_cut of each particle; the momentum gather of the same step
+// reads it instead of walking the cells again (the pairs are the same: positions do not
+// change between the two gathers).  Entry k of particle i is e[k * stride + i] =
+// (j - i) << 9 | (dz + m) << 6 | (dy + m) << 3 | (dx + m): j the sorted index of the
+// neighbour, (dx, dy, dz) the offset of j's cell from i's cell, m the reach in cells.
+// n[i] = the number of entries, or kListWalk when they do not fit (more than kmax
+// neighbours, j - i outside 23 bits, or m > 3): momentum then walks the cells for i.
+struct NbrList {
+    int32_t* e;
+    int32_t* n;
+    int32_t kmax;
+    int64_t stride;
+};
+constexpr int32_t kListWalk = 0x7fffffff;
+constexpr int32_t kListDelta = 1 << 22;  // |j - i| < kListDelta
 
 struct SortScratch {
     int32_t* key;    // per particle (unsorted index): global cell key or kDeadKey

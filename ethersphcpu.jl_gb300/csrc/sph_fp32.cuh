@@ -44,11 +44,45 @@ struct Kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// x^n for n >= 0 by repeated squaring, without the compensation of jl_powi.
+__device__ __forceinline__ double powi_plain(double x, int n) {
+    double y = 1.0;
+    while (n > 0) {
+        if (n & 1) y *= x;
+        x *= x;
+        n >>= 1;
+    }
+    return y;
+}
+
 template <int TPP>
 __device__ __forceinline__ unsigned group_mask() {
     if (TPP == 32) return 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     return ((1u << TPP) - 1u) << (lane & ~(unsigned)(TPP - 1));
+}
+
+// Combine the compensated sums of a particle's TPP lanes in place: the lanes' (s, c)
+// pairs are merged in FP32 (the sums by an error-free TwoSum whose rounding error joins
+// the compensations); every lane ends with the same bits, and one lane converts the
+// result with value() (FP64 work is slow on GB300: done once per particle).
+template <int TPP>
+__device__ __forceinline__ void group_combine(Kahan& k, unsigned mask) {
+#pragma unroll
+    for (int o = TPP / 2; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(mask, k.s, o);
+        const float c2 = __shfl_xor_sync(mask, k.c, o);
+        const float t = k.s + s2;
+        const float bp = t - k.s;
+        const float e = (k.s - (t - bp)) + (s2 - bp);
+        k.s = t;
+        k.c = (k.c + c2) - e;
+    }
+}
+
+// Non-finite test on the exponent bits (integer work instead of FP64 compares).
+__device__ __forceinline__ bool bits_finite(double x) {
+    return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000;
 }
 
 template <int TPP>
@@ -146,6 +180,19 @@ __device__ __forceinline__ int run_dx(const RowRun& R, int j) {
     return R.dx0 + (j >= R.bnd[0]) + (j >= R.bnd[1]) + (j >= R.bnd[2]) + (j >= R.bnd[3]);
 }
 
+// Cell offset of a candidate in metres, and its neighbour-list code (see NbrList).
+// The product is rounded on its own (no contraction into the caller's subtraction), so
+// the cell walk and the list walk form bitwise the same pair vectors.
+__device__ __forceinline__ float cell_offset(int d, float edge) { return __fmul_rn((float)d, edge); }
+__device__ __forceinline__ int row_code(int dy, int dz, int m) { return ((dz + m) << 6) | ((dy + m) << 3); }
+
+// |r|^2 with a fixed rounding sequence: the continuity gather's test and the momentum
+// gather's test agree bit for bit, so the neighbour list holds exactly the pairs the
+// momentum walk would accept.
+__device__ __forceinline__ float dist2(float rx, float ry, float rz) {
+    return __fmaf_rn(rx, rx, __fmaf_rn(ry, ry, __fmul_rn(rz, rz)));
+}
+
 template <int DIM, int TPP, typename F>
 __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
                                            int lane, F&& f) {
@@ -158,13 +205,17 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
             const int y = c[1] + dy;
             if (y < 0 || y >= S.n[1]) continue;
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
-            const float oy = (float)dy * S.cell_f[1];
-            const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
+            const float oy = cell_offset(dy, S.cell_f[1]);
+            const float oz = DIM == 3 ? cell_offset(dz, S.cell_f[2]) : 0.f;
+            const int rc = row_code(dy, dz, m) + m;
             // the row's cells are one virtual range v = 0 .. (sum of lengths)-1; lane t
             // takes v = t, t+TPP, ...
             RowRun R;
             if (row_run(S, start, row, c[0], R)) {
-                for (int j = R.b + lane; j < R.e; j += TPP) f(j, (float)run_dx(R, j) * S.cell_f[0], oy, oz);
+                for (int j = R.b + lane; j < R.e; j += TPP) {
+                    const int dx = run_dx(R, j);
+                    f(j, cell_offset(dx, S.cell_f[0]), oy, oz, rc + dx);
+                }
                 continue;
             }
             int prefix = 0;  // a wrapping row of a periodic axis: cell by cell
@@ -173,9 +224,9 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
                 x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
-                const float ox = (float)dx * S.cell_f[0];
+                const float ox = cell_offset(dx, S.cell_f[0]);
                 const int first = (lane - prefix) & (TPP - 1);
-                for (int j = b + first; j < e; j += TPP) f(j, ox, oy, oz);
+                for (int j = b + first; j < e; j += TPP) f(j, ox, oy, oz, rc + dx);
                 prefix += e - b;
             }
         }
@@ -198,8 +249,9 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
             const int y = c[1] + dy;
             if (y < 0 || y >= S.n[1]) continue;
             const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
-            const float oy = (float)dy * S.cell_f[1];
-            const float oz = DIM == 3 ? (float)dz * S.cell_f[2] : 0.f;
+            const float oy = cell_offset(dy, S.cell_f[1]);
+            const float oz = DIM == 3 ? cell_offset(dz, S.cell_f[2]) : 0.f;
+            const int rc = row_code(dy, dz, m) + m;
             RowRun R;
             if (row_run(S, start, row, c[0], R)) {
                 int j = R.b + lane;
@@ -210,7 +262,8 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
                     const bool more = jn < R.e;
                     decltype(d) dn = d;
                     if (more) dn = load(jn);
-                    f(j, d, (float)run_dx(R, j) * S.cell_f[0], oy, oz);
+                    const int dx = run_dx(R, j);
+                    f(j, d, cell_offset(dx, S.cell_f[0]), oy, oz, rc + dx);
                     if (!more) break;
                     j = jn;
                     d = dn;
@@ -223,7 +276,7 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
                 x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
                 const int e = __ldg(start + row + x + 1);
-                const float ox = (float)dx * S.cell_f[0];
+                const float ox = cell_offset(dx, S.cell_f[0]);
                 int j = b + ((lane - prefix) & (TPP - 1));
                 prefix += e - b;
                 if (j >= e) continue;
@@ -233,7 +286,7 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
                     const bool more = jn < e;
                     decltype(d) dn = d;
                     if (more) dn = load(jn);
-                    f(j, d, ox, oy, oz);
+                    f(j, d, ox, oy, oz, rc + dx);
                     if (!more) break;
                     j = jn;
                     d = dn;
@@ -243,16 +296,71 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
     }
 }
 
-// Walk with (PF) or without software pipelining; body(j, load(j), ox, oy, oz).
+// Walk with (PF) or without software pipelining; body(j, load(j), ox, oy, oz, code).
 template <int DIM, int TPP, bool PF, typename L, typename F>
 __device__ __forceinline__ void walk(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
                                      int lane, L&& load, F&& body) {
     if constexpr (PF) {
         walk_lanes_pf<DIM, TPP>(S, start, c, lane, load, body);
     } else {
-        walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz) {
-            body(j, load(j), ox, oy, oz);
+        walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz, int code) {
+            body(j, load(j), ox, oy, oz, code);
         });
+    }
+}
+
+// Entry k of particle i.
+__device__ __forceinline__ const int32_t* list_entry(const NbrList& nl, int k, int i) {
+    return nl.e + (int64_t)k * nl.stride + i;
+}
+
+// Walk of particle i's neighbour list (cnt entries, NbrList): lane t takes entries t,
+// t+TPP, ...; the PF form loads the next entry and its neighbour's data before the
+// current neighbour is processed.  body as for walk().
+template <int DIM, int TPP, bool PF, typename L, typename F>
+__device__ __forceinline__ void walk_list(const SceneDev& S, const NbrList& nl, int i, int cnt, int lane, L&& load,
+                                          F&& body) {
+    const int m = S.reach;
+    auto entry = [&](int k) { return __ldg(list_entry(nl, k, i)); };
+    auto off = [&](int32_t x, float& ox, float& oy, float& oz) {
+        ox = cell_offset((x & 7) - m, S.cell_f[0]);
+        oy = cell_offset(((x >> 3) & 7) - m, S.cell_f[1]);
+        oz = DIM == 3 ? cell_offset(((x >> 6) & 7) - m, S.cell_f[2]) : 0.f;
+    };
+    if constexpr (PF) {
+        int k = lane;
+        if (k >= cnt) return;
+        int32_t x = entry(k);
+        int j = i + (x >> 9);
+        auto d = load(j);
+        for (;;) {
+            const int kn = k + TPP;
+            const bool more = kn < cnt;
+            int32_t xn = x;
+            int jn = j;
+            decltype(d) dn = d;
+            if (more) {
+                xn = entry(kn);
+                jn = i + (xn >> 9);
+                dn = load(jn);
+            }
+            float ox, oy, oz;
+            off(x, ox, oy, oz);
+            body(j, d, ox, oy, oz, 0);
+            if (!more) break;
+            k = kn;
+            x = xn;
+            j = jn;
+            d = dn;
+        }
+    } else {
+        for (int k = lane; k < cnt; k += TPP) {
+            const int32_t x = entry(k);
+            const int j = i + (x >> 9);
+            float ox, oy, oz;
+            off(x, ox, oy, oz);
+            body(j, load(j), ox, oy, oz, 0);
+        }
     }
 }
 
@@ -279,9 +387,11 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 }
 
 // -------------------------------------------------------------------- K4 (FP32)
-template <int DIM, int KK, int TPP, bool PF>
+// LIST (one lane per particle): also records the neighbours within r_cut in nl.
+template <int DIM, int KK, int TPP, bool PF, bool LIST>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
-                                 BufferState bf) {
+                                 BufferState bf, NbrList nl) {
+    static_assert(!LIST || TPP == 1, "the neighbour list is written by one lane per particle");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *sc.n_live) return;
@@ -302,15 +412,34 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
     int32_t c[3];
     decode_cell(st.cell[i], S, c);
     Kahan drho;
+    int cnt = 0;
+    bool list_ok = !LIST || S.reach <= 3;
+    int32_t* lp = LIST ? nl.e + i : nullptr;
+    if (LIST) {  // every candidate lies between the first and the last neighbour row
+        const int m = S.reach;
+        const int zl = DIM == 3 ? max(c[2] - m, 0) : 0, zh = DIM == 3 ? min(c[2] + m, S.n[2] - 1) : 0;
+        const int lo = __ldg(start + S.cell_off + (zl * S.n[1] + max(c[1] - m, 0)) * S.n[0]);
+        const int hi = __ldg(start + S.cell_off + (zh * S.n[1] + min(c[1] + m, S.n[1] - 1) + 1) * S.n[0]);
+        list_ok &= i - lo < kListDelta && hi - i <= kListDelta;
+    }
     auto load = [&](int j) { return Cand2{st.fa[j], st.fb[j]}; };
-    walk<DIM, TPP, PF>(S, start, c, lane, load, [&](int j, const Cand2& cd, float ox, float oy, float oz) {
+    walk<DIM, TPP, PF>(S, start, c, lane, load, [&](int j, const Cand2& cd, float ox, float oy, float oz, int code) {
         if (j == i) return;
         const float4 aj = cd.a;
         const float4 bj = cd.b;
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
-        const float d2 = rx * rx + ry * ry + rz * rz;
+        const float d2 = dist2(rx, ry, rz);
         if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
+        if (LIST) {
+            if (cnt < nl.kmax) {
+                *lp = (int32_t)(((uint32_t)(j - i) << 9) | (uint32_t)code);
+                lp += nl.stride;
+            } else {
+                list_ok = false;
+            }
+            ++cnt;
+        }
         const float inv_r = rsqrtf(d2);
         const float r = d2 * inv_r;
         float W, dW;
@@ -330,23 +459,32 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         }
         drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
     });
-    double dr = group_sum<TPP>(drho.value(), group_mask<TPP>());
+    group_combine<TPP>(drho, group_mask<TPP>());
     if (lane != 0) return;
+    double dr = drho.value();
+    if (LIST) {
+        nl.n[i] = list_ok ? cnt : kListWalk;
+    }
     if (bf.n) {  // inlet/outlet buffer neighbours, FP64
         using V = typename VecT<DIM>::T;
         dr += buffer_drho<DIM, KK>(S, bf, c, ((const V*)st.x)[i], ((const V*)st.v)[i]);
     }
+    // Tait equation of state (UpdatePressure.jl:8-16) with one FP64 division and plain
+    // powers: FP64 is slow on GB300, and these values feed FP32 pair terms (P, c) or FP64
+    // sums (vol) where their last-bit differences from the reference's rounding do not show
     double rho = st.rho[i];
     rho += dr * S.dt;
-    const double rr = rho / S.rho0;
-    const double p = S.b * (jl_powi(rr, S.gamma) - 1.0) + S.p0;
-    const double cs = S.c0 * sqrt(jl_powi(rr, S.gamma - 1));
-    const double P = p / (rho * rho);
+    const double inv_rho = 1.0 / rho;
+    const double rr = rho * S.inv_rho0;
+    const double p = S.b * (powi_plain(rr, S.gamma) - 1.0) + S.p0;
+    const double cs =
+        S.c0 * ((S.gamma & 1) ? powi_plain(rr, (S.gamma - 1) >> 1) : sqrt(powi_plain(rr, S.gamma - 1)));
+    const double P = p * inv_rho * inv_rho;
     st.rhoc[i] = rho;
     st.p[i] = p;
     st.c[i] = cs;
     st.P[i] = P;
-    st.vol[i] = st.m[i] / rho;
+    st.vol[i] = st.m[i] * inv_rho;
     if (DIM == 2) {
         const float4 bi = st.fb[i];
         st.fb[i] = make_float4(bi.x, (float)rho, (float)P, bi.w);
@@ -364,9 +502,12 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
 // neighbour loads on large scenes (about 10% faster at 1M particles), at the cost of a
 // few spilled bytes in the thermal variant.  The pipelined walk keeps its registers (its
 // prefetched candidate would spill) and is therefore limited to blocks of 256 threads.
-template <int DIM, int KK, int MODE, int TPP, bool PF>
+// LIST: the fluid neighbours come from the list the continuity gather recorded (the
+// cell walk for a particle whose list did not fit).
+template <int DIM, int KK, int MODE, int TPP, bool PF, bool LIST>
 __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
-                               SortScratch sc, int32_t cap, BufferState bf, BufferScratch bs, BufferRules br) {
+                               SortScratch sc, int32_t cap, BufferState bf, BufferScratch bs, BufferRules br,
+                               NbrList nl) {
     using V = typename VecT<DIM>::T;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
@@ -416,15 +557,14 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         d.c = (DIM == 3 || MODE == kModeThermal) ? st.fc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         return d;
     };
-    walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, [&](int j, const Cand3& cd, float ox, float oy,
-                                                              float oz) {
+    auto pair = [&](int j, const Cand3& cd, float ox, float oy, float oz, int) {
         if (j == i) return;
         const float4 aj = cd.a;
         const float4 bj = cd.b;
         const float4 cj = cd.c;
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
-        const float d2 = rx * rx + ry * ry + rz * rz;
+        const float d2 = dist2(rx, ry, rz);
         if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
         const float inv_r = rsqrtf(d2);
         const float r = d2 * inv_r;
@@ -463,7 +603,14 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
             const float dq = __fdividef(2.f * keq * r * dW, rho_i * rho_j * (r * r + S.hh001_f)) * (T_i - T_j);
             dT.add(dq * m_j * inv_cp_i);
         }
-    });
+    };
+    if constexpr (LIST) {
+        const int cnt = nl.n[i];
+        if (cnt != kListWalk) walk_list<DIM, TPP, PF>(S, nl, i, cnt, lane, load_f, pair);
+        else walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, pair);
+    } else {
+        walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, pair);
+    }
 
     if (wl.n > 0) {
         auto load_w = [&](int w) {
@@ -475,7 +622,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
             return d;
         };
         walk<DIM, TPP, PF>(S, wl.start, c, lane, load_w, [&](int w, const WallCand& cd, float ox, float oy,
-                                                                   float oz) {
+                                                                   float oz, int) {
             const float4 wa = cd.a;
             const float4 wb = cd.b;
             const float4 wc = cd.c;
@@ -550,11 +697,14 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     }
 
     const unsigned mask = group_mask<TPP>();
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) group_combine<TPP>(dv[k], mask);
+    if (MODE == kModeThermal) group_combine<TPP>(dT, mask);
+    if (lane != 0) return;
     double dvd[DIM];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) dvd[k] = group_sum<TPP>(dv[k].value(), mask);
-    const double dTd = MODE == kModeThermal ? group_sum<TPP>(dT.value(), mask) : 0.0;
-    if (lane != 0) return;
+    for (int k = 0; k < DIM; ++k) dvd[k] = dv[k].value();
+    const double dTd = MODE == kModeThermal ? dT.value() : 0.0;
 
     // ---- FP64 forward Euler on the masters (UpdateTemperature/Velocity/Position.jl)
     const int64_t step = sc.scene_step[s];
@@ -587,7 +737,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     for (int k = 0; k < DIM; ++k) {
         vn[k] += body[k] * dt;
         vn[k] += dvd[k] * dt;
-        xn[k] += vn[k] * dt - dvd[k] * S.dtdt / 2.0;
+        xn[k] += vn[k] * dt - dvd[k] * S.half_dtdt;  // dv dt^2 / 2
     }
     if (S.periodic_x) {
         if (xn[0] >= S.wrap_hi) xn[0] -= S.period;
@@ -605,9 +755,9 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     const double rho_d = st.rhoc[i];
     nx.rho[i] = rho_d;
 
-    bool finite = isfinite(rho_d);
+    bool finite = bits_finite(rho_d);
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) finite &= isfinite(xn[k]) & isfinite(vn[k]);
+    for (int k = 0; k < DIM; ++k) finite &= bits_finite(xn[k]) & bits_finite(vn[k]);
     if (!finite && S.nan_check) atomicOr(sc.status, kStatusNonFinite);
     bool dead = false;
     if (S.check_enabled && is_step(step, S.check_interval)) {
@@ -647,12 +797,12 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
     double sw = 0.0, sws = 0.0;
     auto load = [&](int j) { return CandShep{st.fa[j], st.vol[j], st.m[j]}; };
     walk<DIM, TPP, PF>(S, sc.start, c, lane, load, [&](int j, const CandShep& cd, float ox, float oy,
-                                                            float oz) {
+                                                            float oz, int) {
         if (j == i) return;
         const float4 aj = cd.a;
         const float rx = xi0 - ox - aj.x, ry = xi1 - oy - aj.y;
         const float rz = DIM == 3 ? xi2 - oz - aj.z : 0.f;
-        const float d2 = rx * rx + ry * ry + rz * rz;
+        const float d2 = dist2(rx, ry, rz);
         if (!(d2 <= S.rc2_f)) return;
         const double W = (double)kernel_w_f<KK>(sqrtf(d2) * S.inv_h_f, S);
         sw += W * cd.vol;
@@ -668,51 +818,70 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
 }
 
 // -------------------------------------------------------------------- launchers
-template <int DIM, int KK, int TPP, bool PF>
+template <int DIM, int KK, int TPP, bool PF, bool LIST>
 void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        k_continuity_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap, L.bf);
+        if constexpr (!LIST || TPP == 1)
+            k_continuity_f32<DIM, KK, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap, L.bf,
+                                                                                    L.nl);
     } else if (stage == 2) {
-        k_reinit_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap,
-                                                                      L.force_reinit);
+        if constexpr (!LIST)
+            k_reinit_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap,
+                                                                          L.force_reinit);
     } else if (mode == kModeFluidWall) {
-        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
+        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else if (mode == kModeWallPressure) {
-        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
+        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else if (mode == kModeBuffers) {
-        k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
+        k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else {
-        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br);
+        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
+            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     }
 }
 
 // Lanes code: 1, 2, 4, 8 lanes per particle; -1: one lane with a software-pipelined
-// candidate loop (pays off when few warps are resident, i.e. small scenes).
-template <int DIM, int KK>
+// candidate loop (pays off when few warps are resident, i.e. small scenes).  The cell
+// walks (LIST false) take every code for every stage; with the neighbour list (LIST
+// true) continuity runs one lane (1 or -1) and momentum 1, 2, 4 or -1 lanes.
+template <int DIM, int KK, bool LIST>
 void launch_kk(int stage, const LaunchCtx& L) {
     const int tpp = stage == 0 ? L.tpp_continuity : (stage == 1 ? L.tpp_momentum : L.tpp_reinit);
-    switch (tpp) {
-        case -1: launch_tpp<DIM, KK, 1, true>(stage, L.mode, L); break;
-        case 1: launch_tpp<DIM, KK, 1, false>(stage, L.mode, L); break;
-        case 2: launch_tpp<DIM, KK, 2, false>(stage, L.mode, L); break;
-        case 8: launch_tpp<DIM, KK, 8, false>(stage, L.mode, L); break;
-        default: launch_tpp<DIM, KK, 4, false>(stage, L.mode, L); break;
+    if constexpr (LIST) {
+        if (stage == 0) {
+            if (tpp == -1) launch_tpp<DIM, KK, 1, true, true>(stage, L.mode, L);
+            else launch_tpp<DIM, KK, 1, false, true>(stage, L.mode, L);
+            return;
+        }
+        switch (tpp) {
+            case -1: launch_tpp<DIM, KK, 1, true, true>(stage, L.mode, L); break;
+            case 1: launch_tpp<DIM, KK, 1, false, true>(stage, L.mode, L); break;
+            case 2: launch_tpp<DIM, KK, 2, false, true>(stage, L.mode, L); break;
+            default: launch_tpp<DIM, KK, 4, false, true>(stage, L.mode, L); break;
+        }
+    } else {
+        switch (tpp) {
+            case -1: launch_tpp<DIM, KK, 1, true, false>(stage, L.mode, L); break;
+            case 1: launch_tpp<DIM, KK, 1, false, false>(stage, L.mode, L); break;
+            case 2: launch_tpp<DIM, KK, 2, false, false>(stage, L.mode, L); break;
+            case 8: launch_tpp<DIM, KK, 8, false, false>(stage, L.mode, L); break;
+            default: launch_tpp<DIM, KK, 4, false, false>(stage, L.mode, L); break;
+        }
     }
 }
 
-template <int DIM>
+template <int DIM, bool LIST>
 void dispatch(int stage, const LaunchCtx& L) {
     switch (L.kernel) {
-        case SPH_KERNEL_CUBIC_SPLINE: launch_kk<DIM, SPH_KERNEL_CUBIC_SPLINE>(stage, L); break;
-        case SPH_KERNEL_GAUSSIAN: launch_kk<DIM, SPH_KERNEL_GAUSSIAN>(stage, L); break;
-        case SPH_KERNEL_WENDLAND_C2: launch_kk<DIM, SPH_KERNEL_WENDLAND_C2>(stage, L); break;
-        default: launch_kk<DIM, SPH_KERNEL_WENDLAND_C4>(stage, L); break;
+        case SPH_KERNEL_CUBIC_SPLINE: launch_kk<DIM, SPH_KERNEL_CUBIC_SPLINE, LIST>(stage, L); break;
+        case SPH_KERNEL_GAUSSIAN: launch_kk<DIM, SPH_KERNEL_GAUSSIAN, LIST>(stage, L); break;
+        case SPH_KERNEL_WENDLAND_C2: launch_kk<DIM, SPH_KERNEL_WENDLAND_C2, LIST>(stage, L); break;
+        default: launch_kk<DIM, SPH_KERNEL_WENDLAND_C4, LIST>(stage, L); break;
     }
 }
 

@@ -28,6 +28,10 @@ struct LaunchCtx {
     // launch shape of the FP32 gathers (lanes per particle, threads per block)
     int block;
     int tpp_continuity, tpp_momentum, tpp_reinit;
+    // list_momentum != 0: continuity (one lane) records the neighbour list and momentum
+    // reads it (tpp_momentum lanes per particle)
+    int list_momentum;
+    NbrList nl;
     // inlet/outlet buffers (bf.n == nullptr: none): current and next sorted buffers
     BufferState bf, bf2;
     BufferScratch bs;
@@ -40,6 +44,8 @@ void launch_physics_fp64(int stage, const LaunchCtx& L);
 void launch_physics_fp32(int stage, const LaunchCtx& L);
 void launch_physics_fp32_2d(int stage, const LaunchCtx& L);
 void launch_physics_fp32_3d(int stage, const LaunchCtx& L);
+void launch_physics_fp32_list_2d(int stage, const LaunchCtx& L);
+void launch_physics_fp32_list_3d(int stage, const LaunchCtx& L);
 
 // Buffer particles after the gathers of a step (K4-K6): move them, copy inlet particles
 // that crossed into the fluid, move the fluid particles K5 marked to the outlet, drop

@@ -157,6 +157,64 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __res
     }
 }
 
+// Down-sweep that forms its tile's offset itself from the tile sums of k_scan_tiles (a
+// block reduction over the tiles before it): two launches instead of three for grids of
+// at most kScanDirectTiles tiles.  Block 0 also writes the total and advances the steps.
+constexpr int kScanDirectTiles = 64;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t* __restrict__ count, int32_t n,
+                                                                  const int32_t* __restrict__ tile_sums,
+                                                                  int32_t ntiles, int32_t* __restrict__ start,
+                                                                  int32_t* __restrict__ n_next,
+                                                                  int64_t* __restrict__ scene_step, int32_t nscenes,
+                                                                  int advance) {
+    __shared__ int32_t tile[kScanTile];
+    __shared__ int32_t warp_sums[kScanThreads / 32];
+    __shared__ int32_t offset;
+    const int base = blockIdx.x * kScanTile;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = k * kScanThreads + threadIdx.x;
+        tile[idx] = base + idx < n ? count[base + idx] : 0;
+    }
+    if (threadIdx.x < 32) {  // offset of this tile: sum of the tile sums before it
+        const int upto = blockIdx.x == 0 ? ntiles : blockIdx.x;  // block 0: the total
+        int32_t t = 0;
+        for (int q = threadIdx.x; q < upto; q += 32) t += tile_sums[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) {
+            offset = blockIdx.x == 0 ? 0 : t;
+            if (blockIdx.x == 0) {
+                start[n] = t;
+                *n_next = t;
+            }
+        }
+    }
+    if (blockIdx.x == 0 && advance)
+        for (int q = threadIdx.x; q < nscenes; q += blockDim.x) scene_step[q] += 1;
+    __syncthreads();
+    int32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) local += tile[threadIdx.x * kScanItems + k];
+    int32_t total;
+    int32_t run = block_exclusive_scan<kScanThreads>(local, warp_sums, &total) + offset;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = threadIdx.x * kScanItems + k;
+        const int32_t c = tile[idx];
+        tile[idx] = run;
+        run += c;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = k * kScanThreads + threadIdx.x;
+        if (base + idx < n) start[base + idx] = tile[idx];
+    }
+}
+
 // ---------------------------------------------------------------- placement
 __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -317,32 +375,65 @@ void launch_hash(const LaunchCtx& L) {
     else k_hash<3><<<grid, 128, 0, L.stream>>>(L.scenes, L.nx, L.st, L.sc, L.cap);
 }
 
-// Whole scan in one block when the grid has at most 1024 x 16 cells.
+// Whole scan in one block, chunk by chunk (1024 x 16 cells each) with a running carry,
+// when the grid has at most kScanSingleChunks chunks: one launch.  One block moves the
+// whole array through one SM, so more chunks are faster as two launches over many SMs
+// (about 3.4 us per chunk against 10 us for two or three launches on GB300).
+constexpr int kScanChunk = kScanTopThreads * kScanTopItems;
+constexpr int kScanSingleChunks = 1;
+
 __global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* __restrict__ count, int32_t n,
                                                                 int32_t* __restrict__ start,
                                                                 int32_t* __restrict__ n_next,
                                                                 int64_t* __restrict__ scene_step, int32_t nscenes,
                                                                 int advance) {
     __shared__ int32_t warp_sums[kScanTopThreads / 32];
-    int32_t v[kScanTopItems];
-    int32_t local = 0;
+    int32_t carry = 0;
+    for (int base = 0; base < n; base += kScanChunk) {
+        // a thread's 16 cells are 64 contiguous bytes: four 16-byte loads and stores
+        // (count and start are cudaMalloc'd, the thread's first cell a multiple of 16)
+        const int first = base + threadIdx.x * kScanTopItems;
+        const bool whole = first + kScanTopItems <= n;
+        int32_t v[kScanTopItems];
+        int32_t local = 0;
+        if (whole) {
 #pragma unroll
-    for (int k = 0; k < kScanTopItems; ++k) {
-        const int idx = threadIdx.x * kScanTopItems + k;
-        v[k] = idx < n ? count[idx] : 0;
-        local += v[k];
-    }
-    int32_t total;
-    int32_t run = block_exclusive_scan<kScanTopThreads>(local, warp_sums, &total);
+            for (int q = 0; q < kScanTopItems / 4; ++q) {
+                const int4 w = reinterpret_cast<const int4*>(count + first)[q];
+                v[4 * q] = w.x;
+                v[4 * q + 1] = w.y;
+                v[4 * q + 2] = w.z;
+                v[4 * q + 3] = w.w;
+            }
+        } else {
 #pragma unroll
-    for (int k = 0; k < kScanTopItems; ++k) {
-        const int idx = threadIdx.x * kScanTopItems + k;
-        if (idx < n) start[idx] = run;
-        run += v[k];
+            for (int k = 0; k < kScanTopItems; ++k) v[k] = first + k < n ? count[first + k] : 0;
+        }
+#pragma unroll
+        for (int k = 0; k < kScanTopItems; ++k) local += v[k];
+        int32_t total;
+        int32_t run = block_exclusive_scan<kScanTopThreads>(local, warp_sums, &total) + carry;
+#pragma unroll
+        for (int k = 0; k < kScanTopItems; ++k) {
+            const int32_t c = v[k];
+            v[k] = run;
+            run += c;
+        }
+        if (whole) {
+#pragma unroll
+            for (int q = 0; q < kScanTopItems / 4; ++q)
+                reinterpret_cast<int4*>(start + first)[q] = make_int4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanTopItems; ++k)
+                if (first + k < n) start[first + k] = v[k];
+        }
+        carry += total;
+        __syncthreads();  // warp_sums is rewritten by the next chunk
     }
     if (threadIdx.x == 0) {
-        start[n] = total;
-        *n_next = total;
+        start[n] = carry;
+        *n_next = carry;
     }
     if (advance)
         for (int s = threadIdx.x; s < nscenes; s += blockDim.x) scene_step[s] += 1;
@@ -350,13 +441,18 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* 
 
 void launch_scan(const LaunchCtx& L, int advance) {
     const int n = L.total_cells;
-    if (n <= kScanTopThreads * kScanTopItems) {
+    if (n <= kScanSingleChunks * kScanChunk) {
         k_scan_single<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.count, n, L.sc.start, L.n_next, L.sc.scene_step,
                                                            L.nscenes, advance);
         return;
     }
     const int ntiles = (n + kScanTile - 1) / kScanTile;
     k_scan_tiles<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
+    if (ntiles <= kScanDirectTiles) {
+        k_scan_down_direct<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, ntiles, L.sc.start,
+                                                                  L.n_next, L.sc.scene_step, L.nscenes, advance);
+        return;
+    }
     k_scan_top<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
                                                     L.sc.scene_step, L.nscenes, advance);
     k_scan_down<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, L.sc.start);

@@ -300,19 +300,32 @@ int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double
 
 /* Autotuner of the FP32-compensated form: times the continuity, momentum and Shepard
  * gathers on the current state for every lanes-per-particle count {-1, 1, 2, 4, 8} and
- * block size {64, 128, 256}, keeps the fastest for each stage and rebuilds the step
- * graphs.  out[4] (may be NULL) receives (continuity lanes, momentum lanes, Shepard
- * lanes, block size).  The fluid state is left unchanged.  No-op for the FP64 form,
- * which keeps one thread per particle so that its summation order is fixed. */
+ * block size {64, 128, 256}, and the neighbour-list pair (continuity recording the list
+ * with lanes {-1, 1}, momentum reading it with lanes {-1, 1, 2, 4}); keeps the faster of
+ * the cell-walk and list pairs, the fastest Shepard shape, and rebuilds the step graphs.
+ * out[4] (may be NULL) receives (continuity lanes, momentum lanes, Shepard lanes, block
+ * size).  The fluid state is left unchanged.  No-op for the FP64 form, which keeps one
+ * thread per particle so that its summation order is fixed. */
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
+
+/* Momentum lanes code of the neighbour list: SPH_LANES_LIST + t, t in {1, 2, 4, -1}.
+ * The continuity gather (one lane per particle) records, in its walk order, every
+ * neighbour within r_cut of each particle, and the momentum gather of the same step reads
+ * that list with t lanes per particle instead of walking the cells a second time (same
+ * pairs: positions do not change between the two gathers).  The list holds about
+ * 1.25 x the lattice neighbour count of the finest uploaded spacing per particle
+ * (4 bytes each, grown with the live particle count); a particle with more neighbours
+ * walks the cells. */
+#define SPH_LANES_LIST 16
 
 /* Set the FP32 launch shape by hand (a new handle starts at (1, 1, 1, 128)):
  * shape[4] = (continuity lanes, momentum lanes,
  * Shepard lanes, block size); lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
  * is software-pipelined: loads of the next neighbour overlap the current one's
  * arithmetic; momentum lanes -1 take blocks of at most 256), block in {32, 64, ..., 1024}
- * and a multiple of 32.  Results of the FP32
- * form depend on the lanes code (the order of the compensated partial sums, and for -1
+ * and a multiple of 32.  Momentum lanes may instead be a neighbour-list code
+ * (SPH_LANES_LIST + 1, 2, 4 or -1; continuity lanes 1 or -1 then).  Results of the FP32
+ * form depend on the lanes codes (the order of the compensated partial sums, and for -1
  * against 1 the compiler's contraction of a*b+c into fused multiply-adds), never on the
  * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
