@@ -876,7 +876,7 @@ int32_t allocate_handle(SphHandle* h, int64_t cells) {
         size_t n;
     } ints[] = {{&h->sc.key, (size_t)h->cap},        {&h->sc.slot, (size_t)h->cap},
                 {&h->sc.tmp, (size_t)h->cap},        {&h->sc.count, ncell},
-                {&h->sc.start, ncell + 1},           {&h->sc.block_sums, ncell / 4096 + 2},
+                {&h->sc.start, ncell + 1},           {&h->sc.block_sums, ncell / 1024 + 2},
                 {&h->sc.status, 1},                  {&h->nbuf, 2},
                 {&h->W.start, ncell + 1},            {&h->W.kind, wc}};
     for (auto& a : ints)
@@ -987,7 +987,7 @@ int32_t allocate_buffers(SphHandle* h, int64_t cap) {
         int32_t** p;
         size_t n;
     } ints[] = {{&S.key, n}, {&S.slot, n}, {&S.count, ncell}, {&S.start, ncell + 1},
-                {&S.block_sums, ncell / 4096 + 2}, {&S.pend, n}, {&S.npend, 1}, {&h->bn, 2}};
+                {&S.block_sums, ncell / 1024 + 2}, {&S.pend, n}, {&S.npend, 1}, {&h->bn, 2}};
     for (auto& a : ints)
         if ((e = dalloc(h, a.p, a.n)) != cudaSuccess) return cuda_fail(h, e, "buffer scratch");
     if ((e = dalloc(h, &S.tmp, n)) != cudaSuccess) return cuda_fail(h, e, "buffer scratch");

@@ -73,13 +73,14 @@ __device__ __forceinline__ int32_t block_exclusive_scan(int32_t v, int32_t* warp
     return warp_prefix + inc - v;
 }
 
+template <int ITEMS>
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ count, int32_t n,
                                                             int32_t* __restrict__ tile_sums) {
     __shared__ int32_t red[kScanThreads / 32];
-    const int base = blockIdx.x * kScanTile;
+    const int base = blockIdx.x * kScanThreads * ITEMS;
     int32_t s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
+    for (int k = 0; k < ITEMS; ++k) {
         const int idx = base + k * kScanThreads + threadIdx.x;
         s += idx < n ? count[idx] : 0;
     }
@@ -159,8 +160,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __res
 
 // Down-sweep that forms its tile's offset itself from the tile sums of k_scan_tiles (a
 // block reduction over the tiles before it): two launches instead of three for grids of
-// at most kScanDirectTiles tiles.  Block 0 also writes the total and advances the steps.
-constexpr int kScanDirectTiles = 64;
+// at most kScanDirectTiles tiles of kScanDirectItems x 256 cells (small tiles: many
+// blocks in flight on a small grid).  Block 0 also writes the total and advances the
+// steps.
+constexpr int kScanDirectItems = 4;
+constexpr int kScanDirectTile = kScanThreads * kScanDirectItems;
+constexpr int kScanDirectTiles = 256;
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t* __restrict__ count, int32_t n,
                                                                   const int32_t* __restrict__ tile_sums,
@@ -168,12 +173,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t
                                                                   int32_t* __restrict__ n_next,
                                                                   int64_t* __restrict__ scene_step, int32_t nscenes,
                                                                   int advance) {
-    __shared__ int32_t tile[kScanTile];
+    constexpr int ITEMS = kScanDirectItems;
+    __shared__ int32_t tile[kScanDirectTile];
     __shared__ int32_t warp_sums[kScanThreads / 32];
     __shared__ int32_t offset;
-    const int base = blockIdx.x * kScanTile;
+    const int base = blockIdx.x * kScanDirectTile;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
+    for (int k = 0; k < ITEMS; ++k) {
         const int idx = k * kScanThreads + threadIdx.x;
         tile[idx] = base + idx < n ? count[base + idx] : 0;
     }
@@ -196,20 +202,20 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t
     __syncthreads();
     int32_t local = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) local += tile[threadIdx.x * kScanItems + k];
+    for (int k = 0; k < ITEMS; ++k) local += tile[threadIdx.x * ITEMS + k];
     int32_t total;
     int32_t run = block_exclusive_scan<kScanThreads>(local, warp_sums, &total) + offset;
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        const int idx = threadIdx.x * kScanItems + k;
+    for (int k = 0; k < ITEMS; ++k) {
+        const int idx = threadIdx.x * ITEMS + k;
         const int32_t c = tile[idx];
         tile[idx] = run;
         run += c;
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
+    for (int k = 0; k < ITEMS; ++k) {
         const int idx = k * kScanThreads + threadIdx.x;
         if (base + idx < n) start[base + idx] = tile[idx];
     }
@@ -446,13 +452,15 @@ void launch_scan(const LaunchCtx& L, int advance) {
                                                            L.nscenes, advance);
         return;
     }
-    const int ntiles = (n + kScanTile - 1) / kScanTile;
-    k_scan_tiles<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
-    if (ntiles <= kScanDirectTiles) {
-        k_scan_down_direct<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, ntiles, L.sc.start,
+    const int dtiles = (n + kScanDirectTile - 1) / kScanDirectTile;
+    if (dtiles <= kScanDirectTiles) {
+        k_scan_tiles<kScanDirectItems><<<dtiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
+        k_scan_down_direct<<<dtiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, dtiles, L.sc.start,
                                                                   L.n_next, L.sc.scene_step, L.nscenes, advance);
         return;
     }
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tiles<kScanItems><<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
     k_scan_top<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
                                                     L.sc.scene_step, L.nscenes, advance);
     k_scan_down<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, L.sc.start);
