@@ -36,6 +36,8 @@ WALL_STATIC_VELOCITY = 1
 WALL_THERMOSTATIC = 2
 PRECISION_FP64 = 0
 PRECISION_FP32_COMPENSATED = 1
+# momentum lanes codes SPH_LANES_LIST + t (t in 1, 2, 4, -1) read the neighbour list
+LANES_LIST = 16
 NUM_STAGES = 6
 STAGE_NAMES = ["cell_count", "scan", "sort", "continuity", "momentum", "reinit"]
 

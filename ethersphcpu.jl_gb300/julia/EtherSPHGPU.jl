@@ -187,7 +187,7 @@ outputWrite(h, file_step, t) =
 outputFlush(h) = checkStatus(h, ccall((:sph_output_flush, libsph), Int32, (Ptr{Cvoid},), h))
 
 function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, check, aabb, precision, domain,
-    periodic_x, staged_output)
+    periodic_x, staged_output, autotune = false)
     if domain === nothing
         pts = reduce(hcat, [stack(g, :x_vec_) for g in [[fluid]; wall_groups] if !isempty(g)])
         pad = 2 * kernel.influence_radius_
@@ -202,6 +202,10 @@ function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, ch
     try
         foreach(g -> uploadWalls(h[], g), wall_groups)
         uploadFluid(h[], fluid)
+        if autotune && precision == FP32Compensated  # launch shape picked on this scene
+            checkStatus(h[], ccall((:sph_autotune, libsph), Int32, (Ptr{Cvoid}, Int32, Ptr{Int32}), h[], Int32(3),
+                C_NULL))
+        end
         if staged
             openOutput(h[], vtp_io)
             outputWrite(h[], 0, 0.0)
@@ -246,10 +250,10 @@ function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidPartic
     wall_particles::AbstractVector{<:WallParticle}, smooth_kernel::SmoothKernel,
     wc_lm::WeaklyCompressibleLiquidModel, dr_fti_forward_euler::DensityReinitializedFixedTimeIntervalForwardEuler,
     vtp_io::VTPIO; check::Function = defaultCheck, aabb = nothing, precision = FP64, domain = nothing,
-    periodic_x::Bool = false, staged_output::Bool = true)::Nothing
+    periodic_x::Bool = false, staged_output::Bool = true, autotune::Bool = false)::Nothing
     code = solveCode(wall_particles)
     return runSolve!(code, fluid_particles, [wall_particles], smooth_kernel, wc_lm, dr_fti_forward_euler, vtp_io,
-        check, aabb, precision, domain, periodic_x, staged_output)
+        check, aabb, precision, domain, periodic_x, staged_output, autotune)
 end
 
 # FluidCompulsiveThermostaticWallSolve.jl:154-233
@@ -259,9 +263,9 @@ function EtherSPHCPU.solve!(::GPU, fluid_particles::AbstractVector{<:FluidPartic
     th_wc_lm::ThermalWeaklyCompressibleLiquidModel,
     dr_fti_forward_euler::DensityReinitializedFixedTimeIntervalForwardEuler, vtp_io::VTPIO;
     check::Function = defaultCheck, aabb = nothing, precision = FP64, domain = nothing,
-    staged_output::Bool = true)::Nothing
+    staged_output::Bool = true, autotune::Bool = false)::Nothing
     return runSolve!(Int32(2), fluid_particles, [wall_particles, thermostatic_wall_particles], smooth_kernel,
-        th_wc_lm, dr_fti_forward_euler, vtp_io, check, aabb, precision, domain, false, staged_output)
+        th_wc_lm, dr_fti_forward_euler, vtp_io, check, aabb, precision, domain, false, staged_output, autotune)
 end
 
 # ---------------------------------------------------------------- inlet / outlet

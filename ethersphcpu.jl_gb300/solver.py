@@ -275,7 +275,7 @@ def _variant(walls):
 
 def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: int = _abi.PRECISION_FP64,
           domain_lo=None, domain_hi=None, periodic_x: bool = False, first_step: int = 1, nsteps: int | None = None,
-          staged_output: bool = True, wall_time: str | None = None):
+          staged_output: bool = True, wall_time: str | None = None, autotune: bool = False):
     """GPU counterpart of solve!(fluid, walls..., kernel, model, td, vtp_io; check).
 
     Runs steps first_step .. td.total_step_ (or `nsteps` steps), writes VTP files at
@@ -284,7 +284,9 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
     files from device snapshots while the next steps run; otherwise every output step
     downloads the state and writes the file here.  `domain_lo/hi` bound the cell grid
     (default: the particles' bounding box grown by two cut-off radii; particles leaving
-    it are clamped into the edge cells, which stays exact but slower).
+    it are clamped into the edge cells, which stays exact but slower).  `autotune` picks
+    the FP32-compensated form's launch shape on the uploaded scene (sph_autotune); the
+    form's results depend on the shape in the last bits, so it is off by default.
     """
     *walls, kernel, model, td = args
     for w in walls:
@@ -302,6 +304,8 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
         for w in walls:
             sim.upload_walls(w)
         sim.upload_fluid(fluid)
+        if autotune and precision == _abi.PRECISION_FP32_COMPENSATED:
+            sim.autotune(3)
         staged = vtp_io is not None and staged_output
         if staged:
             sim.output_open(vtp_io, wall_time)

@@ -29,6 +29,14 @@ def test_header_declares_the_entry_points():
         assert required in names
 
 
+def test_python_constants_match_the_header():
+    from ethersph_gb300 import _abi
+    text = "".join(h.read_text() for h in HEADERS)
+    defines = dict(re.findall(r"^#define\s+(SPH_\w+)\s+(-?\d+)\s*$", text, flags=re.M))
+    assert int(defines["SPH_LANES_LIST"]) == _abi.LANES_LIST
+    assert int(defines["SPH_NUM_STAGES"]) == _abi.NUM_STAGES
+
+
 def test_library_exports_every_declared_symbol(pkg):
     from ethersph_gb300 import _abi
     lib = _abi.load_library()

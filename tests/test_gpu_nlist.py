@@ -14,7 +14,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-LIST = 16  # SPH_LANES_LIST
+LIST = 16  # SPH_LANES_LIST (_abi.LANES_LIST)
 
 
 def rel(a, b):
@@ -131,3 +131,16 @@ def test_autotune_may_pick_the_list(pkg):
         assert shape[0] in (-1, 1)
     for k in before:
         assert np.array_equal(before[k], after[k]), k
+
+
+def test_solve_with_autotune_follows_fp64(pkg):
+    # solve(...; precision=FP32-compensated, autotune=True): the launch shape is picked
+    # on the uploaded scene (cell walk or list) and the result stays within the form's bar
+    sc = scenes_mod()
+    a = sc.natural_convection_2d(n=64, total_step=200)
+    b = sc.natural_convection_2d(n=64, total_step=200)
+    pkg.solve(a.fluid, *a.walls, a.kernel, a.model, a.td, domain_lo=a.domain_lo, domain_hi=a.domain_hi)
+    pkg.solve(b.fluid, *b.walls, b.kernel, b.model, b.td, domain_lo=b.domain_lo, domain_hi=b.domain_hi,
+              precision=1, autotune=True)
+    for k in ("rho_", "v_vec_", "x_vec_", "t_"):
+        assert rel(getattr(b.fluid, k), getattr(a.fluid, k)) <= 1e-4, k
