@@ -591,6 +591,48 @@ int32_t set_scene_step(SphHandle* h, int s, int64_t step) {
 
 // Write the walls of scene s (host copy) into its region: sorted by (cell, upload
 // index), with the scene's wall cell starts and FP32 shadows.
+// Cells of a scene whose neighbour box (+-reach cells per axis, x wrapping on a periodic
+// axis) holds a wall particle: the only cells whose particles need the wall walk.
+// `start` is the scene's wall start array (ncells + 1 entries); the sentinel cell gets 0.
+std::vector<uint8_t> wall_near_cells(const SceneDev& S, int dim, const std::vector<int32_t>& start) {
+    const int64_t nx = S.n[0], ny = S.n[1], nz = dim == 3 ? S.n[2] : 1, m = S.reach;
+    const int64_t ncells = nx * ny * nz;
+    std::vector<uint8_t> a(ncells + 1, 0), b(ncells + 1, 0);
+    for (int64_t c = 0; c < ncells; ++c) a[c] = start[c + 1] > start[c];
+    // dilate by +-m along x, then y, then z
+    for (int64_t row = 0; row < ny * nz; ++row)
+        for (int64_t x = 0; x < nx; ++x) {
+            uint8_t v = 0;
+            for (int64_t d = -m; d <= m && !v; ++d) {
+                int64_t q = x + d;
+                if (S.periodic_x) q = (q % nx + nx) % nx;
+                else if (q < 0 || q >= nx) continue;
+                v = a[row * nx + q];
+            }
+            b[row * nx + x] = v;
+        }
+    for (int64_t z = 0; z < nz; ++z)
+        for (int64_t y = 0; y < ny; ++y)
+            for (int64_t x = 0; x < nx; ++x) {
+                uint8_t v = 0;
+                for (int64_t d = -m; d <= m && !v; ++d)
+                    if (y + d >= 0 && y + d < ny) v = b[(z * ny + y + d) * nx + x];
+                a[(z * ny + y) * nx + x] = v;
+            }
+    if (dim == 3) {
+        for (int64_t z = 0; z < nz; ++z)
+            for (int64_t c = 0; c < nx * ny; ++c) {
+                uint8_t v = 0;
+                for (int64_t d = -m; d <= m && !v; ++d)
+                    if (z + d >= 0 && z + d < nz) v = a[(z + d) * nx * ny + c];
+                b[z * nx * ny + c] = v;
+            }
+        a.swap(b);
+    }
+    a[ncells] = 0;
+    return a;
+}
+
 int32_t write_scene_walls(SphHandle* h, int s) {
     SceneRec& R = h->scenes[s];
     const SceneDev& S = R.dev;
@@ -666,6 +708,8 @@ int32_t write_scene_walls(SphHandle* h, int s) {
         }
     }
     SPH_CUDA(h, cudaMemcpyAsync(h->W.start + S.cell_off, start.data(), start.size() * 4, cudaMemcpyHostToDevice, st));
+    const std::vector<uint8_t> near = wall_near_cells(S, dim, start);
+    SPH_CUDA(h, cudaMemcpyAsync(h->W.near + S.cell_off, near.data(), near.size(), cudaMemcpyHostToDevice, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));
     R.wall_n = nw;
     return SPH_OK;
@@ -881,6 +925,7 @@ int32_t allocate_handle(SphHandle* h, int64_t cells) {
                 {&h->W.start, ncell + 1},            {&h->W.kind, wc}};
     for (auto& a : ints)
         if ((e = dalloc(h, a.p, a.n)) != cudaSuccess) return cuda_fail(nullptr, e, "scratch");
+    if ((e = dalloc(h, &h->W.near, ncell + 1)) != cudaSuccess) return cuda_fail(nullptr, e, "scratch");
     if ((e = dalloc(h, &h->sc.scene_step, (size_t)h->scap)) != cudaSuccess) return cuda_fail(nullptr, e, "steps");
     if ((e = dalloc(h, &h->d_scenes, (size_t)h->scap)) != cudaSuccess) return cuda_fail(nullptr, e, "scenes");
     if ((e = alloc_vec(h, &h->W.x, wc)) != cudaSuccess) return cuda_fail(nullptr, e, "walls");

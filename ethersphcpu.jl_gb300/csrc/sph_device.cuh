@@ -130,6 +130,7 @@ struct WallState {
     double* kappa;
     int32_t* kind;
     int32_t* start;  // global cells + 1
+    uint8_t* near;   // global cells: 1 where a wall particle lies within +-reach cells
     float4* fa;      // FP32: 2D (xr, yr, nx, ny)    3D (xr, yr, zr, gap)
     float4* fb;      // FP32: 2D (vx, vy, gap, T)    3D (nx, ny, nz, T)
     float4* fc;      // FP32: 2D (kappa, kind, -, -) 3D (vx, vy, vz, kappa)

@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, pair);
     }
 
-    if (wl.n > 0) {
+    if (wl.n > 0 && wl.near[st.cell[i]]) {  // walls only where a wall cell is within reach
         auto load_w = [&](int w) {
             WallCand d;
             d.a = wl.fa[w];
