@@ -327,6 +327,8 @@ struct SphHandle {
     sph::VtpWriter* out = nullptr;  // VTP output (sph_output_open)
     double* probe_buf = nullptr;    // device points + results of sph_probe
     int64_t probe_cap = 0;          // doubles in probe_buf
+    char* dl_buf = nullptr;         // device staging of downloads (row order + gathered fields)
+    size_t dl_cap = 0;              // bytes in dl_buf
     int64_t out_walls = -1;         // wall groups the writer holds
 };
 
@@ -805,7 +807,35 @@ int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const dou
     return resort(h);
 }
 
-// Download the live particles of scene s in ascending id.
+// Row order of a download: positions of the sorted particles in ascending id (the
+// caller's original order with deleted particles removed).  Ids are unique and small
+// (upload indices, then inlet copies): a position table, linear in n; a sort otherwise.
+void ascending_id_order(const std::vector<int32_t>& ids, std::vector<int32_t>& order) {
+    const int64_t n = (int64_t)ids.size();
+    order.resize(n);
+    int32_t lo = INT32_MAX, hi = -1;
+    for (int32_t id : ids) {
+        lo = std::min(lo, id);
+        hi = std::max(hi, id);
+    }
+    if (n > 0 && lo >= 0 && (int64_t)hi <= 8 * n + 1024) {
+        std::vector<int32_t> pos((size_t)hi + 1, -1);
+        for (int64_t k = 0; k < n; ++k) pos[ids[k]] = (int32_t)k;
+        int64_t q = 0;
+        for (int32_t id = 0; id <= hi; ++id)
+            if (pos[id] >= 0) {
+                if (q == n) break;
+                order[q++] = pos[id];
+            }
+        if (q == n) return;  // unique ids: done
+    }
+    for (int64_t k = 0; k < n; ++k) order[k] = (int32_t)k;
+    std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return ids[a] < ids[b]; });
+}
+
+// Download the live particles of scene s in ascending id: the rows are put in that order
+// on the device (one gather launch into a staging buffer), then each requested array is
+// copied straight into the caller's memory.
 int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, double* x, double* v, double* rho,
                        double* p, double* c, double* mass, double* gap, double* t, double* kappa, double* cp,
                        int64_t* ids_out) {
@@ -819,41 +849,49 @@ int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, do
     cudaStream_t st = h->stream;
     const int dim = h->dim;
     const SortedState& d = h->S[h->par];
-    const size_t vb = vec_bytes(dim);
-    std::vector<int32_t> ids(n);
+    std::vector<int32_t> ids(n), order;
     SPH_CUDA(h, cudaMemcpyAsync(ids.data(), d.id + b, n * 4, cudaMemcpyDeviceToHost, st));
-    std::vector<char> bx, bv;
-    std::vector<double> b1[8];
+    SPH_CUDA(h, cudaStreamSynchronize(st));
+    ascending_id_order(ids, order);
+    if (ids_out)
+        for (int64_t q = 0; q < n; ++q) ids_out[q] = ids[order[q]];
     const double* srcs[8] = {d.rho, d.p, d.c, d.m, d.gap, d.T, d.kappa, d.cp};
     double* dsts[8] = {rho, p, c, mass, gap, t, kappa, cp};
+    DownloadFields F{};
+    F.x = x != nullptr;
+    F.v = v != nullptr;
+    double* out_of[8] = {};
+    for (int f = 0; f < 8; ++f)
+        if (dsts[f] && srcs[f]) {
+            out_of[F.n] = dsts[f];
+            F.src[F.n++] = srcs[f];
+        }
+    if (!F.x && !F.v && F.n == 0) return SPH_OK;
+    const size_t cols = (size_t)(F.x + F.v) * dim + (size_t)F.n;
+    const size_t need = (size_t)n * 4 + 16 + (size_t)n * cols * 8;
+    if (need > h->dl_cap) {
+        if (h->dl_buf) cudaFree(h->dl_buf);
+        h->dl_buf = nullptr;
+        h->dl_cap = 0;
+        SPH_CUDA(h, cudaMalloc((void**)&h->dl_buf, need));
+        h->dl_cap = need;
+    }
+    int32_t* d_order = (int32_t*)h->dl_buf;
+    double* d_out = (double*)(h->dl_buf + (((size_t)n * 4 + 15) / 16) * 16);
+    SPH_CUDA(h, cudaMemcpyAsync(d_order, order.data(), n * 4, cudaMemcpyHostToDevice, st));
+    launch_gather_rows(st, dim, d_order, n, b, d.x, d.v, F, d_out);
+    SPH_CUDA(h, cudaGetLastError());
+    double* o = d_out;
     if (x) {
-        bx.resize(n * vb);
-        SPH_CUDA(h, cudaMemcpyAsync(bx.data(), (const char*)d.x + (size_t)b * vb, n * vb, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(h, cudaMemcpyAsync(x, o, (size_t)n * dim * 8, cudaMemcpyDeviceToHost, st));
+        o += n * dim;
     }
     if (v) {
-        bv.resize(n * vb);
-        SPH_CUDA(h, cudaMemcpyAsync(bv.data(), (const char*)d.v + (size_t)b * vb, n * vb, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(h, cudaMemcpyAsync(v, o, (size_t)n * dim * 8, cudaMemcpyDeviceToHost, st));
+        o += n * dim;
     }
-    for (int f = 0; f < 8; ++f) {
-        if (!dsts[f] || !srcs[f]) continue;
-        b1[f].resize(n);
-        SPH_CUDA(h, cudaMemcpyAsync(b1[f].data(), srcs[f] + b, n * 8, cudaMemcpyDeviceToHost, st));
-    }
+    for (int f = 0; f < F.n; ++f) SPH_CUDA(h, cudaMemcpyAsync(out_of[f], o + (size_t)f * n, n * 8, cudaMemcpyDeviceToHost, st));
     SPH_CUDA(h, cudaStreamSynchronize(st));
-    // ascending id = the caller's original order with deleted particles removed
-    std::vector<int64_t> order(n);
-    for (int64_t k = 0; k < n; ++k) order[k] = k;
-    std::sort(order.begin(), order.end(), [&](int64_t a, int64_t q) { return ids[a] < ids[q]; });
-    for (int64_t q = 0; q < n; ++q) {
-        const int64_t k = order[q];
-        for (int a = 0; a < dim; ++a) {
-            if (x) x[q * dim + a] = ((const double*)(bx.data() + k * vb))[a];
-            if (v) v[q * dim + a] = ((const double*)(bv.data() + k * vb))[a];
-        }
-        for (int f = 0; f < 8; ++f)
-            if (dsts[f] && srcs[f]) dsts[f][q] = b1[f][k];
-        if (ids_out) ids_out[q] = ids[k];
-    }
     return SPH_OK;
 }
 
@@ -1939,6 +1977,11 @@ int32_t sph_destroy(SphHandle* h) {
         if (h->stream) cudaStreamSynchronize(h->stream);
         cudaFree(h->probe_buf);
         h->probe_buf = nullptr;
+    }
+    if (h->dl_buf) {
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        cudaFree(h->dl_buf);
+        h->dl_buf = nullptr;
     }
     if (h->out) {
         std::string err;

@@ -59,6 +59,16 @@ void launch_hash(const LaunchCtx& L);
 void launch_scan(const LaunchCtx& L, int advance);
 // Stable (cell, id) placement: tmp fill, then rank + copy of every field into L.st2.
 void launch_place(const LaunchCtx& L);
+// Fields of a download: x and v (flags) and up to 8 FP64 per-particle arrays.
+struct DownloadFields {
+    int x, v;
+    int n;
+    const double* src[8];
+};
+// Gather rows b + order[q], q < n, of the sorted state into out (device): x (n x dim)
+// and v (n x dim) when flagged, then one n-array per field.
+void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int64_t n, int32_t b, const void* x,
+                        const void* v, const DownloadFields& F, double* out);
 // FP64 reductions: out[0] = sum m, out[1] = sum m|v|^2/2, out[2] = max |v|.
 void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out);
 // Unique fluid pairs (sorted j > i) and fluid-wall pairs within r_cut.

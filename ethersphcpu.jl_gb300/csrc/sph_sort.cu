@@ -466,6 +466,40 @@ void launch_scan(const LaunchCtx& L, int advance) {
     k_scan_down<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, L.sc.start);
 }
 
+// Rows of a download in the caller's order: row q takes sorted particle b + order[q];
+// out = x (n x dim), v (n x dim), then one n-array per requested field.
+template <int DIM>
+__global__ void k_gather_rows(const int32_t* __restrict__ order, int64_t n, int32_t b, const void* __restrict__ x,
+                              const void* __restrict__ v, DownloadFields F, double* __restrict__ out) {
+    using V = typename VecT<DIM>::T;
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int64_t k = b + order[q];
+    double* o = out;
+    if (F.x) {
+        const V xv = ((const V*)x)[k];
+        o[q * DIM] = xv.x;
+        o[q * DIM + 1] = xv.y;
+        if constexpr (DIM == 3) o[q * DIM + 2] = xv.z;
+        o += n * DIM;
+    }
+    if (F.v) {
+        const V vv = ((const V*)v)[k];
+        o[q * DIM] = vv.x;
+        o[q * DIM + 1] = vv.y;
+        if constexpr (DIM == 3) o[q * DIM + 2] = vv.z;
+        o += n * DIM;
+    }
+    for (int f = 0; f < F.n; ++f) o[f * n + q] = F.src[f][k];
+}
+
+void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int64_t n, int32_t b, const void* x,
+                        const void* v, const DownloadFields& F, double* out) {
+    const int grid = (int)((n + 255) / 256);
+    if (dim == 2) k_gather_rows<2><<<grid, 256, 0, stream>>>(order, n, b, x, v, F, out);
+    else k_gather_rows<3><<<grid, 256, 0, stream>>>(order, n, b, x, v, F, out);
+}
+
 void launch_place(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
     k_fill<<<grid, 128, 0, L.stream>>>(L.sc, L.st.id, L.cap);
