@@ -472,7 +472,11 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
     // Tait equation of state (UpdatePressure.jl:8-16) with one FP64 division and plain
     // powers: FP64 is slow on GB300, and these values feed FP32 pair terms (P, c) or FP64
     // sums (vol) where their last-bit differences from the reference's rounding do not show
+    // loads first: stores to the state arrays would otherwise order them (possible aliasing)
     double rho = st.rho[i];
+    const double m_i = st.m[i];
+    const float4 fb_i = st.fb[i];
+    const float4 fc_i = DIM == 3 ? st.fc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     rho += dr * S.dt;
     const double inv_rho = 1.0 / rho;
     const double rr = rho * S.inv_rho0;
@@ -484,15 +488,12 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
     st.p[i] = p;
     st.c[i] = cs;
     st.P[i] = P;
-    st.vol[i] = st.m[i] * inv_rho;
+    st.vol[i] = m_i * inv_rho;
     if (DIM == 2) {
-        const float4 bi = st.fb[i];
-        st.fb[i] = make_float4(bi.x, (float)rho, (float)P, bi.w);
+        st.fb[i] = make_float4(fb_i.x, (float)rho, (float)P, fb_i.w);
     } else {
-        const float4 bi = st.fb[i];
-        st.fb[i] = make_float4(bi.x, bi.y, bi.z, (float)rho);
-        const float4 ci = st.fc[i];
-        st.fc[i] = make_float4((float)P, ci.y, ci.z, ci.w);
+        st.fb[i] = make_float4(fb_i.x, fb_i.y, fb_i.z, (float)rho);
+        st.fc[i] = make_float4((float)P, fc_i.y, fc_i.z, fc_i.w);
     }
 }
 
@@ -710,8 +711,9 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     const int64_t step = sc.scene_step[s];
     const V x0 = ((const V*)st.x)[i];
     const V v0 = ((const V*)st.v)[i];
+    const double rho_d = st.rhoc[i];  // loaded before the stores below (possible aliasing)
     if (MODE == kModeBuffers && bf.n) {  // inlet/outlet buffer neighbours, FP64
-        const double rho_d = st.rhoc[i], gap_d = st.gap[i];
+        const double gap_d = st.gap[i];
         buffer_dv<DIM, KK>(S, bf, c, x0, v0, rho_d, st.P[i], gap_d, kernel_w<KK>(gap_d, S), S.nu0 * rho_d, dvd);
     }
     const double dt = S.dt;
@@ -752,7 +754,6 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     }
     ((V*)nx.x)[i] = xo;
     ((V*)nx.v)[i] = vo;
-    const double rho_d = st.rhoc[i];
     nx.rho[i] = rho_d;
 
     bool finite = bits_finite(rho_d);

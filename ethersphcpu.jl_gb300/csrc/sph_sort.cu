@@ -240,51 +240,54 @@ __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, Ne
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t key = sc.key[i];
     if (key == kDeadKey) return;
+    // every source element is loaded before the first store: the compiler cannot prove
+    // that the destination arrays do not alias the sources, and would otherwise order
+    // each load after the previous store (one memory round trip per field)
+    const V x = ((const V*)nx.x)[i];
+    const V v = ((const V*)nx.v)[i];
+    const double rho = nx.rho[i], p = src.p[i], c = src.c[i], m = src.m[i], gap = src.gap[i];
+    const int32_t myid = src.id[i], scn = src.scene[i];
+    double T = 0.0, kap = 0.0, cpv = 1.0;
+    if (THERMAL) {
+        T = nx.T[i];
+        kap = src.kappa[i];
+        cpv = src.cp[i];
+    }
     const int32_t b = sc.start[key], e = sc.start[key + 1];
-    const int32_t myid = src.id[i];
     int32_t rank = 0;
     for (int32_t t = b; t < e; ++t) rank += sc.tmp[t] < myid;
     const int32_t d = b + rank;
-    ((V*)dst.x)[d] = ((const V*)nx.x)[i];
-    ((V*)dst.v)[d] = ((const V*)nx.v)[i];
-    dst.rho[d] = nx.rho[i];
-    dst.p[d] = src.p[i];
-    dst.c[d] = src.c[i];
-    dst.m[d] = src.m[i];
-    dst.gap[d] = src.gap[i];
+    ((V*)dst.x)[d] = x;
+    ((V*)dst.v)[d] = v;
+    dst.rho[d] = rho;
+    dst.p[d] = p;
+    dst.c[d] = c;
+    dst.m[d] = m;
+    dst.gap[d] = gap;
     dst.id[d] = myid;
-    dst.scene[d] = src.scene[i];
+    dst.scene[d] = scn;
     if (THERMAL) {
-        dst.T[d] = nx.T[i];
-        dst.kappa[d] = src.kappa[i];
-        dst.cp[d] = src.cp[i];
+        dst.T[d] = T;
+        dst.kappa[d] = kap;
+        dst.cp[d] = cpv;
     }
     if (SHADOW) {  // FP32 shadows: position relative to the origin of the particle's cell
-        const SceneDev& S = scenes[src.scene[i]];
+        const SceneDev& S = scenes[scn];
         const int32_t k = key - S.cell_off;
         const int32_t cx = k % S.n[0], cy = (k / S.n[0]) % S.n[1], cz = k / (S.n[0] * S.n[1]);
-        const V x = ((const V*)nx.x)[i];
-        const V v = ((const V*)nx.v)[i];
         const float xr = (float)(x.x - __dadd_rn(S.lo[0], __dmul_rn((double)cx, S.cell_d[0])));
         const float yr = (float)(x.y - __dadd_rn(S.lo[1], __dmul_rn((double)cy, S.cell_d[1])));
-        const float m = (float)src.m[i], rho = (float)nx.rho[i], gap = (float)src.gap[i];
-        float T = 0.f, kap = 0.f, cpv = 1.f;
-        if (THERMAL) {
-            T = (float)nx.T[i];
-            kap = (float)src.kappa[i];
-            cpv = (float)src.cp[i];
-        }
         dst.cell[d] = key;
         if constexpr (DIM == 2) {
             dst.fa[d] = make_float4(xr, yr, (float)v.x, (float)v.y);
-            dst.fb[d] = make_float4(m, rho, 0.f, gap);
-            dst.fc[d] = make_float4(T, kap, cpv, 0.f);
+            dst.fb[d] = make_float4((float)m, (float)rho, 0.f, (float)gap);
+            dst.fc[d] = make_float4((float)T, (float)kap, (float)cpv, 0.f);
         } else {
             const float zr = (float)(x.z - __dadd_rn(S.lo[2], __dmul_rn((double)cz, S.cell_d[2])));
-            dst.fa[d] = make_float4(xr, yr, zr, m);
-            dst.fb[d] = make_float4((float)v.x, (float)v.y, (float)v.z, rho);
-            dst.fc[d] = make_float4(0.f, gap, T, kap);
-            dst.fd[d] = cpv;
+            dst.fa[d] = make_float4(xr, yr, zr, (float)m);
+            dst.fb[d] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)rho);
+            dst.fc[d] = make_float4(0.f, (float)gap, (float)T, (float)kap);
+            dst.fd[d] = (float)cpv;
         }
     }
 }
