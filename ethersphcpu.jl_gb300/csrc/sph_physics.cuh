@@ -99,10 +99,14 @@ __device__ __forceinline__ void make_rvec(const V& xi, const V& xj, const SceneD
     }
 }
 
+// |r|^2 = sum over k ascending of r_k^2, each product and sum rounded on its own (no
+// fused multiply-add in any translation unit): the pair predicate d^2 <= r_cut^2 then
+// decides every pair as the reference's restatement does, also on lattices where pairs
+// sit at exactly r_cut.
 template <int DIM>
 __device__ __forceinline__ double norm_sq(const double rv[DIM]) {
-    double s = rv[0] * rv[0] + rv[1] * rv[1];
-    if (DIM == 3) s += rv[DIM - 1] * rv[DIM - 1];
+    double s = __dadd_rn(__dmul_rn(rv[0], rv[0]), __dmul_rn(rv[1], rv[1]));
+    if (DIM == 3) s = __dadd_rn(s, __dmul_rn(rv[DIM - 1], rv[DIM - 1]));
     return s;
 }
 
