@@ -21,6 +21,16 @@ namespace sph {
 
 constexpr int32_t kDeadKey = 0x7fffffff;
 
+// Programmatic dependent launch between the kernels of a step (launch_dep): the next
+// kernel's launch is prepared while its predecessor in the stream finishes; pdl_wait()
+// blocks until the predecessor grid has completed and its writes are visible (a no-op
+// when the kernel was launched without the attribute).  Every step kernel calls it first,
+// before it touches device memory.  No kernel triggers its dependents early: blocks of the
+// next kernel parked on the wait took SM slots from the tail of the current one (a
+// 65k-particle step on GB300: 0.0652 ms with an early trigger, 0.0642 ms without
+// programmatic launches, 0.0622 ms with the trigger at block exit, as here).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Status bits written by kernels (atomicOr) and read by the host after a step.
 enum : int32_t { kStatusNonFinite = 1, kStatusClamped = 2, kStatusBufferOverflow = 4 };
 

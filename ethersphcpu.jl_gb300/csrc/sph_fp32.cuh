@@ -391,6 +391,7 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 template <int DIM, int KK, int TPP, bool PF, bool LIST>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
                                  BufferState bf, NbrList nl) {
+    pdl_wait();
     static_assert(!LIST || TPP == 1, "the neighbour list is written by one lane per particle");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
@@ -509,6 +510,7 @@ template <int DIM, int KK, int MODE, int TPP, bool PF, bool LIST>
 __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
                                SortScratch sc, int32_t cap, BufferState bf, BufferScratch bs, BufferRules br,
                                NbrList nl) {
+    pdl_wait();
     using V = typename VecT<DIM>::T;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
@@ -784,6 +786,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
 template <int DIM, int KK, int TPP, bool PF>
 __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, SortScratch sc,
                              int32_t cap, int force) {
+    pdl_wait();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *sc.n_live) return;
@@ -825,24 +828,24 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
         if constexpr (!LIST || TPP == 1)
-            k_continuity_f32<DIM, KK, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.sc, L.cap, L.bf,
-                                                                                    L.nl);
+            launch_dep(k_continuity_f32<DIM, KK, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.sc, L.cap,
+                       L.bf, L.nl);
     } else if (stage == 2) {
         if constexpr (!LIST)
-            k_reinit_f32<DIM, KK, TPP, PF><<<grid, block, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap,
-                                                                          L.force_reinit);
+            launch_dep(k_reinit_f32<DIM, KK, TPP, PF>, grid, block, L.stream, L.scenes, L.st, L.nx, L.sc, L.cap,
+                       L.force_reinit);
     } else if (mode == kModeFluidWall) {
-        k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_dep(k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
+                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else if (mode == kModeWallPressure) {
-        k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_dep(k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st,
+                   L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else if (mode == kModeBuffers) {
-        k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_dep(k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
+                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     } else {
-        k_momentum_f32<DIM, KK, kModeThermal, TPP, PF, LIST><<<grid, block, 0, L.stream>>>(
-            L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_dep(k_momentum_f32<DIM, KK, kModeThermal, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
+                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
     }
 }
 

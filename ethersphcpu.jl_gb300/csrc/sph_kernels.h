@@ -1,6 +1,8 @@
 // sph_kernels.h — host-side launch interface of the device kernels (internal).
 #pragma once
 
+#include <utility>
+
 #include "sph_device.cuh"
 
 namespace sph {
@@ -38,6 +40,24 @@ struct LaunchCtx {
     BufferRules br;
     int32_t* bn_next;  // live buffer particles after the buffer sort being built
 };
+
+// Launch a step kernel with programmatic stream serialisation: its launch is prepared
+// while the previous kernel of the stream finishes (it calls pdl_wait first).  Captured
+// into the step graphs as programmatic edges.
+template <typename... P, typename... A>
+inline void launch_dep(void (*kernel)(P...), int grid, int block, cudaStream_t stream, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 // stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init
 void launch_physics_fp64(int stage, const LaunchCtx& L);

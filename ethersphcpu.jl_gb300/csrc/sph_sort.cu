@@ -76,6 +76,7 @@ __device__ __forceinline__ int32_t block_exclusive_scan(int32_t v, int32_t* warp
 template <int ITEMS>
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ count, int32_t n,
                                                             int32_t* __restrict__ tile_sums) {
+    pdl_wait();
     __shared__ int32_t red[kScanThreads / 32];
     const int base = blockIdx.x * kScanThreads * ITEMS;
     int32_t s = 0;
@@ -100,6 +101,7 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_top(int32_t* __restric
                                                              int32_t* __restrict__ n_next,
                                                              int64_t* __restrict__ scene_step, int32_t nscenes,
                                                              int advance) {
+    pdl_wait();
     __shared__ int32_t warp_sums[kScanTopThreads / 32];
     int32_t v[kScanTopItems];
     int32_t local = 0;
@@ -128,6 +130,7 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_top(int32_t* __restric
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __restrict__ count, int32_t n,
                                                            const int32_t* __restrict__ tile_offsets,
                                                            int32_t* __restrict__ start) {
+    pdl_wait();
     __shared__ int32_t tile[kScanTile];
     __shared__ int32_t warp_sums[kScanThreads / 32];
     const int base = blockIdx.x * kScanTile;
@@ -173,6 +176,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t
                                                                   int32_t* __restrict__ n_next,
                                                                   int64_t* __restrict__ scene_step, int32_t nscenes,
                                                                   int advance) {
+    pdl_wait();
     constexpr int ITEMS = kScanDirectItems;
     __shared__ int32_t tile[kScanDirectTile];
     __shared__ int32_t warp_sums[kScanThreads / 32];
@@ -223,6 +227,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down_direct(const int32_t
 
 // ---------------------------------------------------------------- placement
 __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t cap) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t key = sc.key[i];
@@ -233,6 +238,7 @@ __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t c
 template <int DIM, bool THERMAL, bool SHADOW>
 __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, NextState nx, SortedState dst,
                         SortScratch sc, int32_t cap, int32_t ncells) {
+    pdl_wait();
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     // count[] has been scanned: clear it for the next step's arrivals
@@ -396,6 +402,7 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* 
                                                                 int32_t* __restrict__ n_next,
                                                                 int64_t* __restrict__ scene_step, int32_t nscenes,
                                                                 int advance) {
+    pdl_wait();
     __shared__ int32_t warp_sums[kScanTopThreads / 32];
     int32_t carry = 0;
     for (int base = 0; base < n; base += kScanChunk) {
@@ -451,22 +458,22 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* 
 void launch_scan(const LaunchCtx& L, int advance) {
     const int n = L.total_cells;
     if (n <= kScanSingleChunks * kScanChunk) {
-        k_scan_single<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.count, n, L.sc.start, L.n_next, L.sc.scene_step,
-                                                           L.nscenes, advance);
+        launch_dep(k_scan_single, 1, kScanTopThreads, L.stream, L.sc.count, n, L.sc.start, L.n_next, L.sc.scene_step,
+                   L.nscenes, advance);
         return;
     }
     const int dtiles = (n + kScanDirectTile - 1) / kScanDirectTile;
     if (dtiles <= kScanDirectTiles) {
-        k_scan_tiles<kScanDirectItems><<<dtiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
-        k_scan_down_direct<<<dtiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, dtiles, L.sc.start,
-                                                                  L.n_next, L.sc.scene_step, L.nscenes, advance);
+        launch_dep(k_scan_tiles<kScanDirectItems>, dtiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums);
+        launch_dep(k_scan_down_direct, dtiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums, dtiles,
+                   L.sc.start, L.n_next, L.sc.scene_step, L.nscenes, advance);
         return;
     }
     const int ntiles = (n + kScanTile - 1) / kScanTile;
-    k_scan_tiles<kScanItems><<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums);
-    k_scan_top<<<1, kScanTopThreads, 0, L.stream>>>(L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
-                                                    L.sc.scene_step, L.nscenes, advance);
-    k_scan_down<<<ntiles, kScanThreads, 0, L.stream>>>(L.sc.count, n, L.sc.block_sums, L.sc.start);
+    launch_dep(k_scan_tiles<kScanItems>, ntiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums);
+    launch_dep(k_scan_top, 1, kScanTopThreads, L.stream, L.sc.block_sums, ntiles, L.sc.start + n, L.n_next,
+               L.sc.scene_step, L.nscenes, advance);
+    launch_dep(k_scan_down, ntiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums, L.sc.start);
 }
 
 // Rows of a download in the caller's order: row q takes sorted particle b + order[q];
@@ -505,9 +512,9 @@ void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int6
 
 void launch_place(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
-    k_fill<<<grid, 128, 0, L.stream>>>(L.sc, L.st.id, L.cap);
+    launch_dep(k_fill, grid, 128, L.stream, L.sc, L.st.id, L.cap);
 #define SPH_PLACE(D, T, SH) \
-    k_place<D, T, SH><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.st2, L.sc, L.cap, L.total_cells)
+    launch_dep(k_place<D, T, SH>, grid, 128, L.stream, L.scenes, L.st, L.nx, L.st2, L.sc, L.cap, L.total_cells)
     const bool sh = L.precision == SPH_PRECISION_FP32_COMPENSATED;
     if (L.dim == 2) {
         if (L.thermal) { if (sh) SPH_PLACE(2, true, true); else SPH_PLACE(2, true, false); }
