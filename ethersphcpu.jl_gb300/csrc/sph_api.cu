@@ -435,13 +435,17 @@ int32_t ensure_list(SphHandle* h) {
         if (R.used) depth = std::max(depth, R.list_depth);
     const int64_t rows = grid_rows(h);
     if (h->nl.e && rows <= h->nl.stride && depth <= h->nl.kmax) return SPH_OK;
+    // rows grow by half again at least: a serving batch raises its live bound scene by scene
+    int64_t stride = std::max<int64_t>(std::max<int64_t>(rows, h->nl.stride), 1);
+    if (h->nl.e && rows > h->nl.stride)
+        stride = std::max<int64_t>(stride, std::min<int64_t>(h->cap, h->nl.stride + h->nl.stride / 2));
+    depth = std::max(depth, h->nl.kmax);
     SPH_CUDA(h, cudaStreamSynchronize(h->stream));
     if (h->nl.e) cudaFree(h->nl.e);
     if (h->nl.n) cudaFree(h->nl.n);
     h->nl = NbrList{};
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
-    const int64_t stride = std::max<int64_t>(rows, 1);
     cudaError_t e = cudaMalloc((void**)&h->nl.e, (size_t)stride * (size_t)depth * 4);
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->nl.n, (size_t)stride * 4);
     if (e != cudaSuccess) {
