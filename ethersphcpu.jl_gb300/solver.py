@@ -165,13 +165,22 @@ class Simulation:
     def step(self, first_step: int, nsteps: int) -> None:
         self._check(self.lib.sph_step(self.h, first_step, nsteps))
 
-    def download(self, capacity: int | None = None) -> dict:
+    def download(self, capacity: int | None = None, out: dict | None = None) -> dict:
+        """The live fluid in ascending upload index.  `out` (optional): caller arrays to
+        write into (x, v: (capacity, dim); rho p c mass gap [t kappa cp]: (capacity,),
+        C-contiguous float64); the returned arrays are views of their first n rows."""
         cap = capacity if capacity is not None else self.stats().n_fluid
         d = self.dim
-        out = {k: np.empty((cap, d)) for k in ("x", "v")}
         names = ["rho", "p", "c", "mass", "gap"] + (["t", "kappa", "cp"] if self.thermal else [])
-        for k in names:
-            out[k] = np.empty(cap)
+        if out is None:
+            out = {k: np.empty((cap, d)) for k in ("x", "v")}
+            for k in names:
+                out[k] = np.empty(cap)
+        else:
+            for k in ("x", "v"):
+                assert out[k].shape[0] >= cap and out[k].shape[1:] == (d,), k
+            for k in names:
+                assert out[k].shape[0] >= cap, k
         n = C.c_int64()
         ptr = lambda k: _abi.dptr(out[k]) if k in out else None
         self._check(self.lib.sph_download_fluid(self.h, cap, C.byref(n), ptr("x"), ptr("v"), ptr("rho"), ptr("p"),
@@ -180,18 +189,20 @@ class Simulation:
         return {k: a[: n.value] for k, a in out.items()}
 
     def download_into(self, fluid) -> None:
-        r = self.download(len(fluid))
-        n = len(r["rho"])
-        fluid.resize(n)
-        fluid.x_vec_[:] = r["x"]
-        fluid.v_vec_[:] = r["v"]
-        fluid.rho_[:] = r["rho"]
-        fluid.p_[:] = r["p"]
-        fluid.c_[:] = r["c"]
-        fluid.mass_[:] = r["mass"]
-        fluid.gap_[:] = r["gap"]
+        """The live fluid into `fluid`'s own arrays (the library writes them directly), then
+        `fluid` is cut to the live count (deleted particles removed, upload order kept)."""
+        fields = {"x": "x_vec_", "v": "v_vec_", "rho": "rho_", "p": "p_", "c": "c_", "mass": "mass_", "gap": "gap_"}
         if self.thermal:
-            fluid.t_[:] = r["t"]
+            fields.update(t="t_", kappa="kappa_", cp="cp_")
+        out = {k: getattr(fluid, f) for k, f in fields.items()}
+        if all(a.dtype == np.float64 and a.flags.c_contiguous for a in out.values()):
+            n = len(self.download(len(fluid), out=out)["rho"])
+            fluid.resize(n)
+            return
+        r = self.download(len(fluid))
+        fluid.resize(len(r["rho"]))
+        for k, f in fields.items():
+            getattr(fluid, f)[:] = r[k]
 
     def download_ids(self) -> np.ndarray:
         """Original indices (of the last upload) of the live particles, ascending."""
