@@ -116,6 +116,7 @@ SIGNATURES = {
     "sph_batch_free": (C.c_int32, [_H, C.POINTER(C.c_int64)]),
     "sph_autotune": (C.c_int32, [_H, C.c_int32, C.POINTER(C.c_int32)]),
     "sph_set_launch_shape": (C.c_int32, [_H, C.POINTER(C.c_int32)]),
+    "sph_set_stencil_pruning": (C.c_int32, [_H, C.c_int32]),
     "sph_last_error": (C.c_char_p, [_H]),
     "sph_destroy": (C.c_int32, [_H]),
 }

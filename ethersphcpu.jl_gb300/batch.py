@@ -177,6 +177,11 @@ class Batch:
         shape = (C.c_int32 * 4)(continuity, momentum, reinit, block)
         self._check(self.lib.sph_set_launch_shape(self.h, shape))
 
+    def set_stencil_pruning(self, on: bool) -> None:
+        """FP32 walks skip neighbour cells beyond r_cut (default: 3D on, 2D off); the
+        results are bitwise the same either way."""
+        self._check(self.lib.sph_set_stencil_pruning(self.h, 1 if on else 0))
+
     def autotune(self, reps: int = 3) -> tuple:
         out = (C.c_int32 * 4)()
         self._check(self.lib.sph_autotune(self.h, reps, out))

@@ -170,8 +170,11 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.check_interval = p.check_interval;
 
     for (int a = 0; a < 3; ++a) S.cell_f[a] = (float)S.cell_d[a];
+    S.inv_cell_fx = 1.0f / S.cell_f[0];
     S.h_f = (float)p.h;
     S.rc2_f = (float)(rc * rc);
+    S.rc2_prune = S.rc2_f * 1.00001f;
+    S.prune = 1;
     S.hh001_f = (float)S.hh001;
     S.nu0_f = (float)p.nu_0;
     S.P_bg_f = (float)S.P_bg;
@@ -304,6 +307,10 @@ struct SphHandle {
     // neighbour list of the FP32 form (momentum lanes code >= SPH_LANES_LIST - 1): grown
     // on demand to the per-particle grid and the deepest scene (ensure_list)
     NbrList nl{};
+    // stencil pruning of the FP32 walks (sph_set_stencil_pruning); default on in 3D only:
+    // measured on GB300, it saves 4-8% of a 3D step (25 neighbour rows, corner rows and
+    // cells beyond r_cut skipped) and costs 0-7% in 2D (few cells to skip, per-row bounds)
+    int prune = -1;  // -1: by dimension
     std::string err;
     std::vector<SceneRec> scenes;
     RangeAlloc cells, walls;
@@ -1035,6 +1042,7 @@ int32_t open_scene(SphHandle* h, const SphParams& p, int64_t wall_cap, int64_t f
     S.cell_off = (int32_t)coff;
     S.last_step = last_step;
     S.active = 1;
+    S.prune = h->prune >= 0 ? h->prune : (p.dim == 3 ? 1 : 0);
     SceneRec& R = h->scenes[s];
     R = SceneRec();
     R.used = true;
@@ -1689,6 +1697,18 @@ int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
     for (int k = 0; k < 4; ++k) h->tune[k] = shape[k];
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
+    return SPH_OK;
+}
+
+int32_t sph_set_stencil_pruning(SphHandle* h, int32_t on) {
+    if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
+    h->prune = on ? 1 : 0;
+    for (int s = 0; s < h->scap; ++s) {
+        if (!h->scenes[s].used) continue;
+        h->scenes[s].dev.prune = h->prune;
+        if (int32_t rc = upload_scene_const(h, s); rc != SPH_OK) return rc;
+    }
+    SPH_CUDA(h, cudaStreamSynchronize(h->stream));
     return SPH_OK;
 }
 

@@ -44,7 +44,7 @@ struct SceneDev {
     double cell_d[3];   // cell edge per axis; cell c starts at lo + c * cell_d
     int32_t n[3];
     int32_t reach;      // neighbour cells within +-reach (cells per r_cut)
-    int32_t pad_reach;
+    int32_t prune;      // 1: the FP32 walks skip neighbour cells beyond r_cut (row_span)
     int32_t cell_off;   // first global cell of this scene
     int32_t ncells;
     int32_t periodic_x;
@@ -84,7 +84,9 @@ struct SceneDev {
     float cell_f[3];   // cell edge per axis (float)
     float h_f, rc2_f, hh001_f, nu0_f, P_bg_f;
     float kw_a_f, kg_a_f, inv_h_f, c0_f, rho0_f, inv_cp_f, inv_rho0_f;
-    float pad_f[3];
+    float rc2_prune;    // rc2_f * (1 + 1e-5): conservative bound for the stencil pruning
+    float inv_cell_fx;  // 1 / cell_f[0]
+    float pad_f;
 };
 
 // ---------------------------------------------------------------- vector types

@@ -160,11 +160,13 @@ struct RowRun {
 };
 
 __device__ __forceinline__ bool row_run(const SceneDev& S, const int32_t* __restrict__ start, int row, int cx,
-                                        RowRun& R) {
+                                        int xlo, int xhi, RowRun& R) {
+    // a row whose full stencil wraps takes the cell-by-cell path whatever its pruned
+    // span: each row keeps one code path (one inlined copy of the pair terms, one rounding)
     const int m = S.reach;
     if (S.periodic_x && (cx - m < 0 || cx + m >= S.n[0])) return false;
-    const int x0 = cx - m < 0 ? 0 : cx - m;
-    const int x1 = cx + m >= S.n[0] ? S.n[0] - 1 : cx + m;
+    const int x0 = cx + xlo < 0 ? 0 : cx + xlo;
+    const int x1 = cx + xhi >= S.n[0] ? S.n[0] - 1 : cx + xhi;
     R.b = __ldg(start + row + x0);
     R.e = __ldg(start + row + x1 + 1);
     R.dx0 = x0 - cx;
@@ -174,6 +176,52 @@ __device__ __forceinline__ bool row_run(const SceneDev& S, const int32_t* __rest
         R.bnd[q] = cell <= x1 ? __ldg(start + row + cell) : INT_MAX;
     }
     return true;
+}
+
+// The cells of neighbour row (dy, dz) that can hold a particle within r_cut of particle i
+// (cell-relative position xi): offsets [xlo, xhi] in x, or false when none can.  Bounds
+// are taken from the cell extents with a relative margin of 1e-5 on r_cut^2 (far above
+// the FP32 rounding of the pair distance), so only candidates the distance test would
+// reject are skipped and the walk visits the accepted ones in the same order.  Particles
+// outside the domain are clamped into the grid's first and last cells with their true
+// positions: rows on the y/z grid boundary are kept whole, and the first and last x cells
+// are never trimmed away.
+template <int DIM>
+__device__ __forceinline__ bool row_span(const SceneDev& S, const int32_t c[3], const float xi[3], int y, int z,
+                                         int dy, int dz, int& xlo, int& xhi) {
+    const int m = S.reach;
+    xlo = -m;
+    xhi = m;
+    if (!S.prune) return true;
+    if (y == 0 || y == S.n[1] - 1 || (DIM == 3 && (z == 0 || z == S.n[2] - 1))) return true;
+    const float ey = S.cell_f[1];
+    const float gy = fmaxf(fmaxf((float)dy * ey - xi[1], xi[1] - (float)(dy + 1) * ey), 0.f);
+    float g2 = gy * gy;
+    if (DIM == 3) {
+        const float ez = S.cell_f[2];
+        const float gz = fmaxf(fmaxf((float)dz * ez - xi[2], xi[2] - (float)(dz + 1) * ez), 0.f);
+        g2 += gz * gz;
+    }
+    const float rem = S.rc2_prune - g2;
+    if (rem < 0.f) return false;
+    const float w = sqrtf(rem);
+    int lo = (int)floorf((xi[0] - w) * S.inv_cell_fx);
+    int hi = (int)floorf((xi[0] + w) * S.inv_cell_fx);
+    lo = lo < -m ? -m : lo;
+    hi = hi > m ? m : hi;
+    if (!S.periodic_x) {
+        if (c[0] - m <= 0) {
+            lo = -m;
+            hi = hi < -c[0] ? -c[0] : hi;
+        }
+        if (c[0] + m >= S.n[0] - 1) {
+            hi = m;
+            lo = lo > S.n[0] - 1 - c[0] ? S.n[0] - 1 - c[0] : lo;
+        }
+    }
+    xlo = lo;
+    xhi = hi;
+    return lo <= hi;
 }
 
 __device__ __forceinline__ int run_dx(const RowRun& R, int j) {
@@ -195,7 +243,7 @@ __device__ __forceinline__ float dist2(float rx, float ry, float rz) {
 
 template <int DIM, int TPP, typename F>
 __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
-                                           int lane, F&& f) {
+                                           const float xi[3], int lane, F&& f) {
     const int m = S.reach;
     const int zr = DIM == 3 ? m : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
@@ -208,10 +256,12 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
             const float oy = cell_offset(dy, S.cell_f[1]);
             const float oz = DIM == 3 ? cell_offset(dz, S.cell_f[2]) : 0.f;
             const int rc = row_code(dy, dz, m) + m;
+            int xlo, xhi;
+            if (!row_span<DIM>(S, c, xi, y, z, dy, dz, xlo, xhi)) continue;
             // the row's cells are one virtual range v = 0 .. (sum of lengths)-1; lane t
             // takes v = t, t+TPP, ...
             RowRun R;
-            if (row_run(S, start, row, c[0], R)) {
+            if (row_run(S, start, row, c[0], xlo, xhi, R)) {
                 for (int j = R.b + lane; j < R.e; j += TPP) {
                     const int dx = run_dx(R, j);
                     f(j, cell_offset(dx, S.cell_f[0]), oy, oz, rc + dx);
@@ -219,7 +269,7 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
                 continue;
             }
             int prefix = 0;  // a wrapping row of a periodic axis: cell by cell
-            for (int dx = -m; dx <= m; ++dx) {
+            for (int dx = xlo; dx <= xhi; ++dx) {
                 int x = c[0] + dx;
                 x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
@@ -239,7 +289,7 @@ __device__ __forceinline__ void walk_lanes(const SceneDev& S, const int32_t* __r
 // scenes) cannot hide that latency by switching warps.
 template <int DIM, int TPP, typename L, typename F>
 __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* __restrict__ start,
-                                              const int32_t c[3], int lane, L&& load, F&& f) {
+                                              const int32_t c[3], const float xi[3], int lane, L&& load, F&& f) {
     const int m = S.reach;
     const int zr = DIM == 3 ? m : 0;
     for (int dz = -zr; dz <= zr; ++dz) {
@@ -252,8 +302,10 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
             const float oy = cell_offset(dy, S.cell_f[1]);
             const float oz = DIM == 3 ? cell_offset(dz, S.cell_f[2]) : 0.f;
             const int rc = row_code(dy, dz, m) + m;
+            int xlo, xhi;
+            if (!row_span<DIM>(S, c, xi, y, z, dy, dz, xlo, xhi)) continue;
             RowRun R;
-            if (row_run(S, start, row, c[0], R)) {
+            if (row_run(S, start, row, c[0], xlo, xhi, R)) {
                 int j = R.b + lane;
                 if (j >= R.e) continue;
                 auto d = load(j);
@@ -271,7 +323,7 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
                 continue;
             }
             int prefix = 0;  // a wrapping row of a periodic axis: cell by cell
-            for (int dx = -m; dx <= m; ++dx) {
+            for (int dx = xlo; dx <= xhi; ++dx) {
                 int x = c[0] + dx;
                 x = x < 0 ? x + S.n[0] : (x >= S.n[0] ? x - S.n[0] : x);
                 const int b = __ldg(start + row + x);
@@ -299,11 +351,11 @@ __device__ __forceinline__ void walk_lanes_pf(const SceneDev& S, const int32_t* 
 // Walk with (PF) or without software pipelining; body(j, load(j), ox, oy, oz, code).
 template <int DIM, int TPP, bool PF, typename L, typename F>
 __device__ __forceinline__ void walk(const SceneDev& S, const int32_t* __restrict__ start, const int32_t c[3],
-                                     int lane, L&& load, F&& body) {
+                                     const float xi[3], int lane, L&& load, F&& body) {
     if constexpr (PF) {
-        walk_lanes_pf<DIM, TPP>(S, start, c, lane, load, body);
+        walk_lanes_pf<DIM, TPP>(S, start, c, xi, lane, load, body);
     } else {
-        walk_lanes<DIM, TPP>(S, start, c, lane, [&](int j, float ox, float oy, float oz, int code) {
+        walk_lanes<DIM, TPP>(S, start, c, xi, lane, [&](int j, float ox, float oy, float oz, int code) {
             body(j, load(j), ox, oy, oz, code);
         });
     }
@@ -424,7 +476,7 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         list_ok &= i - lo < kListDelta && hi - i <= kListDelta;
     }
     auto load = [&](int j) { return Cand2{st.fa[j], st.fb[j]}; };
-    walk<DIM, TPP, PF>(S, start, c, lane, load, [&](int j, const Cand2& cd, float ox, float oy, float oz, int code) {
+    walk<DIM, TPP, PF>(S, start, c, xi, lane, load, [&](int j, const Cand2& cd, float ox, float oy, float oz, int code) {
         if (j == i) return;
         const float4 aj = cd.a;
         const float4 bj = cd.b;
@@ -610,9 +662,9 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     if constexpr (LIST) {
         const int cnt = nl.n[i];
         if (cnt != kListWalk) walk_list<DIM, TPP, PF>(S, nl, i, cnt, lane, load_f, pair);
-        else walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, pair);
+        else walk<DIM, TPP, PF>(S, sc.start, c, xi, lane, load_f, pair);
     } else {
-        walk<DIM, TPP, PF>(S, sc.start, c, lane, load_f, pair);
+        walk<DIM, TPP, PF>(S, sc.start, c, xi, lane, load_f, pair);
     }
 
     if (wl.n > 0 && wl.near[st.cell[i]]) {  // walls only where a wall cell is within reach
@@ -624,7 +676,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
             d.kind = (DIM == 3 && MODE == kModeThermal) ? wl.kind[w] : 0;
             return d;
         };
-        walk<DIM, TPP, PF>(S, wl.start, c, lane, load_w, [&](int w, const WallCand& cd, float ox, float oy,
+        walk<DIM, TPP, PF>(S, wl.start, c, xi, lane, load_w, [&](int w, const WallCand& cd, float ox, float oy,
                                                                    float oz, int) {
             const float4 wa = cd.a;
             const float4 wb = cd.b;
@@ -800,7 +852,8 @@ __global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st
     decode_cell(st.cell[i], S, c);
     double sw = 0.0, sws = 0.0;
     auto load = [&](int j) { return CandShep{st.fa[j], st.vol[j], st.m[j]}; };
-    walk<DIM, TPP, PF>(S, sc.start, c, lane, load, [&](int j, const CandShep& cd, float ox, float oy,
+    const float xs[3] = {xi0, xi1, xi2};
+    walk<DIM, TPP, PF>(S, sc.start, c, xs, lane, load, [&](int j, const CandShep& cd, float ox, float oy,
                                                             float oz, int) {
         if (j == i) return;
         const float4 aj = cd.a;

@@ -330,6 +330,14 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
 
+/* Stencil pruning of the FP32-compensated walks (default: on for 3D scenes, off for 2D,
+ * where it does not pay on GB300): for each neighbour row
+ * the walk visits only the cells whose extent comes within r_cut of the particle (with a
+ * margin of 1e-5 on r_cut^2), instead of all 2m+1 cells of the (2m+1)^dim stencil.  Only
+ * candidates the distance test would reject are skipped, so with one lane per particle
+ * the results are bitwise the same either way.  No counterpart in the reference. */
+int32_t sph_set_stencil_pruning(SphHandle* h, int32_t on);
+
 /* ---- inlet / outlet buffers ------------------------------------------------------
  * FluidInletOutletWallSolve (src/Solve/FluidInletOutletWallSolve.jl:8-262), for a
  * single-scene handle created with solve = SPH_SOLVE_FLUID_INLET_OUTLET_WALL (fluid,
