@@ -474,7 +474,7 @@ def run_served(args, rank=0, world=1):
     for name, prec, count, steps, seed in runs:
         reqs = distributed.shard(scenes.poisson_stream(rate=args.served_rate, count=count, seed=seed, steps=steps),
                                  rank, world)
-        srv = serve.Server(budget_bytes=150e9 if prec == 1 else 40e9, precision=prec, autotune=True)
+        srv = serve.Server(budget_bytes=150e9 if prec == 1 else 40e9, precision=prec)  # FP32c: list shape
         try:
             rep = srv.run(reqs)
         finally:

@@ -500,8 +500,22 @@ function GPUBatch(prototype::SphParams, particles::Integer, cells::Integer, wall
         Ref(prototype), particles, cells, walls, Int32(scenes), h))
     b = GPUBatch(h[])
     finalizer(close, b)
+    if prototype.precision == FP32Compensated  # the serving loop's shape: the neighbour list, two lanes
+        setLaunchShape!(b, Int32[-1, LANES_LIST + 2, -1, 128])
+    end
     return b
 end
+
+"""
+    setLaunchShape!(b, shape)
+
+sph_set_launch_shape: (continuity lanes, momentum lanes, Shepard lanes, block size) of the
+FP32-compensated form; momentum lanes LANES_LIST + t read the neighbour list.
+"""
+setLaunchShape!(b::GPUBatch, shape::Vector{Int32}) =
+    checkStatus(b.h, ccall((:sph_set_launch_shape, libsph), Int32, (Ptr{Cvoid}, Ptr{Int32}), b.h, shape))
+
+const LANES_LIST = Int32(16)  # SPH_LANES_LIST
 
 function Base.close(b::GPUBatch)
     if b.h != C_NULL

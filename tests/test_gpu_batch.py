@@ -168,9 +168,9 @@ def test_serving_loop_runs_a_poisson_stream(pkg):
 
 
 def serve_alone(pkg, scene, nsteps):
-    from ethersph_gb300 import batch
-    dim = scene.kernel.dim_
+    from ethersph_gb300 import batch, serve
     with batch.Batch(scene.params(precision=1), scene.n_fluid + 10, 500_000, scene.n_wall + 10, 2) as bt:
+        bt.set_launch_shape(*serve.DEFAULT_LAUNCH_SHAPE)  # the server's shape
         sid = bt.add_scene(scene, 1, nsteps)
         steps = 0
         while steps < nsteps:  # the server steps whole bundles of 10; frozen scenes stay put
