@@ -523,7 +523,8 @@ void enqueue_step(SphHandle* h, bool reinit) {
     if (reinit) launch_physics(2, L);
     if (h->has_buffers) launch_buffers(L);  // before the scan advances the step counter
     launch_scan(L, 1);
-    launch_place(L);
+    // fluid made from inlet particles has no FP32 shadows yet: convert everything then
+    launch_place(L, !h->has_buffers);
     h->par ^= 1;
 }
 

@@ -78,7 +78,9 @@ void launch_hash(const LaunchCtx& L);
 // When advance != 0 it also increments every scene's step counter.
 void launch_scan(const LaunchCtx& L, int advance);
 // Stable (cell, id) placement: tmp fill, then rank + copy of every field into L.st2.
-void launch_place(const LaunchCtx& L);
+// carry_shadows: the current state's FP32 shadows are valid (a step), so the FP32 copies
+// of the per-particle constants are carried over instead of converted from FP64.
+void launch_place(const LaunchCtx& L, bool carry_shadows = false);
 // Fields of a download: x and v (flags) and up to 8 FP64 per-particle arrays.
 struct DownloadFields {
     int x, v;

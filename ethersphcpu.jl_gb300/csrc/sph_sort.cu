@@ -235,7 +235,11 @@ __global__ void k_fill(SortScratch sc, const int32_t* __restrict__ id, int32_t c
     sc.tmp[sc.start[key] + sc.slot[i]] = id[i];
 }
 
-template <int DIM, bool THERMAL, bool SHADOW>
+// CARRY (FP32 shadows of a step): the FP32 copies of the per-particle constants (m, gap,
+// kappa, cp) are taken from the particle's current shadows instead of being converted from
+// FP64 again (the FP64 pipe is 1/64 of the FP32 rate on GB300); after an upload the
+// shadows do not exist yet and are converted.
+template <int DIM, bool THERMAL, bool SHADOW, bool CARRY>
 __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, NextState nx, SortedState dst,
                         SortScratch sc, int32_t cap, int32_t ncells) {
     pdl_wait();
@@ -258,6 +262,36 @@ __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, Ne
         T = nx.T[i];
         kap = src.kappa[i];
         cpv = src.cp[i];
+    }
+    // FP32 constants: carried from the current shadows, or converted
+    float m_f, gap_f, kap_f = 0.f, cp_f = 1.f;
+    if constexpr (SHADOW && CARRY) {
+        if constexpr (DIM == 2) {
+            const float4 b = src.fb[i];
+            m_f = b.x;
+            gap_f = b.w;
+            if (THERMAL) {
+                const float4 cc = src.fc[i];
+                kap_f = cc.y;
+                cp_f = cc.z;
+            }
+        } else {
+            const float4 a = src.fa[i];
+            const float4 cc = src.fc[i];
+            m_f = a.w;
+            gap_f = cc.y;
+            if (THERMAL) {
+                kap_f = cc.w;
+                cp_f = src.fd[i];
+            }
+        }
+    } else {
+        m_f = (float)m;
+        gap_f = (float)gap;
+        if (THERMAL) {
+            kap_f = (float)kap;
+            cp_f = (float)cpv;
+        }
     }
     const int32_t b = sc.start[key], e = sc.start[key + 1];
     int32_t rank = 0;
@@ -286,14 +320,14 @@ __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, Ne
         dst.cell[d] = key;
         if constexpr (DIM == 2) {
             dst.fa[d] = make_float4(xr, yr, (float)v.x, (float)v.y);
-            dst.fb[d] = make_float4((float)m, (float)rho, 0.f, (float)gap);
-            dst.fc[d] = make_float4((float)T, (float)kap, (float)cpv, 0.f);
+            dst.fb[d] = make_float4(m_f, (float)rho, 0.f, gap_f);
+            dst.fc[d] = make_float4((float)T, kap_f, cp_f, 0.f);
         } else {
             const float zr = (float)(x.z - __dadd_rn(S.lo[2], __dmul_rn((double)cz, S.cell_d[2])));
-            dst.fa[d] = make_float4(xr, yr, zr, (float)m);
+            dst.fa[d] = make_float4(xr, yr, zr, m_f);
             dst.fb[d] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)rho);
-            dst.fc[d] = make_float4(0.f, (float)gap, (float)T, (float)kap);
-            dst.fd[d] = (float)cpv;
+            dst.fc[d] = make_float4(0.f, gap_f, (float)T, kap_f);
+            dst.fd[d] = cp_f;
         }
     }
 }
@@ -510,19 +544,23 @@ void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int6
     else k_gather_rows<3><<<grid, 256, 0, stream>>>(order, n, b, x, v, F, out);
 }
 
-void launch_place(const LaunchCtx& L) {
+void launch_place(const LaunchCtx& L, bool carry_shadows) {
     const int grid = (L.cap + 127) / 128;
     launch_dep(k_fill, grid, 128, L.stream, L.sc, L.st.id, L.cap);
-#define SPH_PLACE(D, T, SH) \
-    launch_dep(k_place<D, T, SH>, grid, 128, L.stream, L.scenes, L.st, L.nx, L.st2, L.sc, L.cap, L.total_cells)
+#define SPH_PLACE(D, T, SH, CA) \
+    launch_dep(k_place<D, T, SH, CA>, grid, 128, L.stream, L.scenes, L.st, L.nx, L.st2, L.sc, L.cap, L.total_cells)
+#define SPH_PLACE_SH(D, T) \
+    do { if (!sh) SPH_PLACE(D, T, false, false); else if (carry_shadows) SPH_PLACE(D, T, true, true); \
+         else SPH_PLACE(D, T, true, false); } while (0)
     const bool sh = L.precision == SPH_PRECISION_FP32_COMPENSATED;
     if (L.dim == 2) {
-        if (L.thermal) { if (sh) SPH_PLACE(2, true, true); else SPH_PLACE(2, true, false); }
-        else { if (sh) SPH_PLACE(2, false, true); else SPH_PLACE(2, false, false); }
+        if (L.thermal) SPH_PLACE_SH(2, true);
+        else SPH_PLACE_SH(2, false);
     } else {
-        if (L.thermal) { if (sh) SPH_PLACE(3, true, true); else SPH_PLACE(3, true, false); }
-        else { if (sh) SPH_PLACE(3, false, true); else SPH_PLACE(3, false, false); }
+        if (L.thermal) SPH_PLACE_SH(3, true);
+        else SPH_PLACE_SH(3, false);
     }
+#undef SPH_PLACE_SH
 #undef SPH_PLACE
 }
 
