@@ -368,7 +368,7 @@ cudaError_t dalloc(SphHandle* h, T** p, size_t count) {
     return cudaMemsetAsync(q, 0, std::max<size_t>(count, 1) * sizeof(T), h->stream);
 }
 
-size_t vec_bytes(int dim) { return dim == 2 ? sizeof(double2) : sizeof(double4); }
+size_t vec_bytes(int dim) { return dim == 2 ? sizeof(double2) : sizeof(double4_32a); }
 
 cudaError_t alloc_vec(SphHandle* h, void** p, size_t n) {
     const size_t bytes = std::max<size_t>(n, 1) * vec_bytes(h->dim);

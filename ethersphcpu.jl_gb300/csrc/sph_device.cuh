@@ -3,7 +3,7 @@
 // Layout in HBM (one "scene table" entry per independent simulation; a single-scene
 // handle is a table of one):
 //   sorted state S (double-buffered, S <-> S' each step), index = position in
-//   (cell, id) order:  x, v (double2 in 2D, double4 in 3D, w unused), rho, p, c,
+//   (cell, id) order:  x, v (double2 in 2D, 32-byte aligned double4 in 3D, w unused), rho, p, c,
 //   P = p / rho^2, mass, gap, T, kappa, cp, id, scene
 //   step outputs N (unsorted, same index as S): x', v', T', rho'
 //   cell list: count[cells], start[cells + 1] (exclusive scan), key/slot per particle
@@ -92,14 +92,14 @@ struct SceneDev {
 // ---------------------------------------------------------------- vector types
 template <int DIM> struct VecT;
 template <> struct VecT<2> { using T = double2; };
-template <> struct VecT<3> { using T = double4; };
+template <> struct VecT<3> { using T = double4_32a; };  // 32-byte aligned: one 256-bit access
 
 template <int DIM> struct FVec;
 template <> struct FVec<2> { using T = float2; };
 template <> struct FVec<3> { using T = float4; };
 
 __device__ __forceinline__ double comp(const double2& a, int k) { return k == 0 ? a.x : a.y; }
-__device__ __forceinline__ double comp(const double4& a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+__device__ __forceinline__ double comp(const double4_32a& a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
 
 // ---------------------------------------------------------------- state buffers
 struct SortedState {
