@@ -1658,6 +1658,12 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
             h->tune[3] = m_walk.block;
         }
         h->tune[2] = r_walk.tpp;
+        if (!pick_list && h->nl.e) {  // the list storage of the trials is not needed
+            SPH_CUDA(h, cudaStreamSynchronize(st));
+            cudaFree(h->nl.e);
+            if (h->nl.n) cudaFree(h->nl.n);
+            h->nl = NbrList{};
+        }
         // restore what the timed launches touched: p and c, and the arrivals left in
         // count[]; every other field they wrote is rebuilt by the next step before use
         SPH_CUDA(h, cudaMemsetAsync(h->sc.count, 0, sizeof(int32_t) * (size_t)h->scan_cells, st));
