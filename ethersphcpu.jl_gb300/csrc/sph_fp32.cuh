@@ -10,12 +10,15 @@
 // accumulate in FP64 (FP32 kernel values times FP64 volumes and masses).
 //
 // Each particle's neighbour walk is split over TPP consecutive lanes of a warp: lane t
-// takes candidates t, t+TPP, ... of every neighbour row (the three x-cells of a row are
-// one virtual range), keeps its own compensated partial sums, and the lanes combine
-// them with an xor butterfly in FP64 — every lane ends with the bitwise same total, so
-// results are deterministic for a given TPP.  TPP and the block size are launch
-// parameters picked by the autotuner (more lanes per particle = more warps in flight to
-// hide the dependent neighbour loads).
+// takes candidates t, t+TPP, ... of every neighbour row (the x-cells of a row are one
+// virtual range), keeps its own compensated partial sums, and the lanes combine them
+// with an xor butterfly (FP32 TwoSum of the sums, the rounding errors joining the
+// compensations) — every lane ends with the bitwise same total, so results are
+// deterministic for a given TPP.  TPP and the block size are launch parameters picked by
+// the autotuner (more lanes per particle = more warps in flight to hide the dependent
+// neighbour loads).  With the neighbour-list shapes the continuity gather records each
+// particle's accepted neighbours (NbrList) and the momentum gather reads them instead of
+// walking the cells again; the walks may skip cells of a row beyond r_cut (row_span).
 //
 // Same terms, order of walls after fluid, and solve variants as sph_fp64.cu; the
 // formulas follow Continuity.jl, PressureForce.jl, ViscosityForce.jl, WallForce.jl,
