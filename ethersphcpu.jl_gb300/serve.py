@@ -138,9 +138,12 @@ class Server:
                 b = self.batches[dim]
                 while q:
                     r, scene = q[0]
-                    p, c, w = footprint(scene, b.precision)
+                    p, c, w = footprint(scene, self.precision)
                     fr = b.free()
                     if not (p <= fr["particles"] and c <= fr["cells"] and w <= fr["walls"] and fr["scenes"] >= 1):
+                        if not any(d == dim for d, _sid in active):  # an empty batch cannot hold it
+                            raise ValueError(f"request {r.kind} (seed {r.seed}) needs {p} particles, {c} cells and "
+                                             f"{w} walls: more than the {dim}D batch holds ({fr})")
                         break
                     q.popleft()
                     sid = b.add_scene(scene, first_step=1, nsteps=r.nsteps)
