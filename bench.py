@@ -204,8 +204,10 @@ def algorithmic_bytes(scene, precision, stage, list_entries=0.0):
 
 
 def scan_launches(cells):
-    """Kernels of one cell scan (sph_sort.cu launch_scan)."""
-    return 1 if cells <= 16384 else (2 if cells <= 64 * 4096 else 3)
+    """Kernels of a step's cell scan (sph_sort.cu launch_scan): one block up to 16,384
+    cells; up to 262,144 cells one down-sweep (the momentum epilogue sums the 1,024-cell
+    tiles); above, tile sums, top and down-sweep."""
+    return 1 if cells <= 64 * 4096 else 3
 
 
 def grid_cells(scene, precision):
@@ -402,8 +404,8 @@ def run_ours(args, rank, world, local):
         "plain_fp64": other,
         "launch_shape": {"continuity_lanes": launch_shape[0], "momentum_lanes": launch_shape[1],
                          "reinit_lanes": launch_shape[2], "block": launch_shape[3], "chosen_by": chosen_by},
-        # per step: continuity, momentum, scan (1 kernel up to 16,384 cells, 2 up to
-        # 262,144, else 3), fill, placement; plus the Shepard kernel on re-initialisation steps
+        # per step: continuity, momentum, scan (1 kernel up to 262,144 cells, else 3), fill,
+        # placement; plus the Shepard kernel on re-initialisation steps
         "gpu_launches": args.steps * (4 + scan_launches(grid_cells(scene, prec))) + reinit_steps,
         "clocks": clocks,
     }

@@ -517,12 +517,16 @@ void launch_physics(int stage, const LaunchCtx& L) {
 // its density at this step (the kernel decides per scene).
 void enqueue_step(SphHandle* h, bool reinit) {
     LaunchCtx L = make_ctx(h);
-    // count[] was zeroed by the previous placement (or by the last re-sort)
+    // count[] and the tile sums were zeroed by the previous placement (or the last re-sort);
+    // with a tiled scan the momentum epilogue sums the arrivals per tile as well (not with
+    // inlet/outlet buffers, whose transfers add arrivals after it)
+    const bool tiles = !h->has_buffers && scan_uses_tiles(L.total_cells);
+    if (tiles) L.sc.tile_acc = h->sc.block_sums;
     launch_physics(0, L);
     launch_physics(1, L);
     if (reinit) launch_physics(2, L);
     if (h->has_buffers) launch_buffers(L);  // before the scan advances the step counter
-    launch_scan(L, 1);
+    launch_scan(L, 1, tiles);
     // fluid made from inlet particles has no FP32 shadows yet: convert everything then
     launch_place(L, !h->has_buffers);
     h->par ^= 1;

@@ -177,7 +177,20 @@ struct SortScratch {
     int32_t* n_live;    // device scalar: live particles after the last sort
     int32_t* status;    // device scalar: status bits
     int64_t* scene_step;  // per scene: number of the step being run
+    // non-null in a step whose scan runs over 1,024-cell tiles: the momentum epilogue adds
+    // each particle's arrival to its tile's sum here (the scan then skips its tile pass)
+    int32_t* tile_acc;
 };
+
+constexpr int32_t kScanTileCells = 1024;  // cells of a tile of the two-launch scan
+
+// Warp-aggregated count of arrivals per scan tile: lanes landing in one tile add once.
+__device__ __forceinline__ void count_tile(int32_t* tile_acc, int32_t key) {
+    if (!tile_acc) return;
+    const int tile = key / kScanTileCells;
+    const unsigned peers = __match_any_sync(__activemask(), tile);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(tile_acc + tile, __popc(peers));
+}
 
 // ---------------------------------------------------------------- inlet/outlet buffers
 // Buffer particles (FluidInletOutletWallSolve.jl:8-262): fluid particles of the inlet and

@@ -834,6 +834,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         const int32_t key = cell_key<DIM>(xo, S);
         sc.key[i] = key;
         sc.slot[i] = atomicAdd(sc.count + key, 1);
+        count_tile(sc.tile_acc, key);
     }
 }
 

@@ -354,6 +354,7 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
         const int32_t key = cell_key<DIM>(xo, S);
         sc.key[i] = key;
         sc.slot[i] = atomicAdd(sc.count + key, 1);
+        count_tile(sc.tile_acc, key);
     }
 }
 

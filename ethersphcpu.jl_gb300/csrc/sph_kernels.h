@@ -76,7 +76,11 @@ void launch_buffers(const LaunchCtx& L);
 void launch_hash(const LaunchCtx& L);
 // Exclusive scan of sc.count into sc.start; writes the live total to *L.n_next.
 // When advance != 0 it also increments every scene's step counter.
-void launch_scan(const LaunchCtx& L, int advance);
+// tiles_ready: the step's momentum epilogue already summed the arrivals per 1,024-cell
+// tile (sc.tile_acc) and the two-launch scan skips its tile pass.
+void launch_scan(const LaunchCtx& L, int advance, bool tiles_ready = false);
+// True when a scan over n cells runs as tile sums + down-sweep over 1,024-cell tiles.
+bool scan_uses_tiles(int n);
 // Stable (cell, id) placement: tmp fill, then rank + copy of every field into L.st2.
 // carry_shadows: the current state's FP32 shadows are valid (a step), so the FP32 copies
 // of the per-particle constants are carried over instead of converted from FP64.

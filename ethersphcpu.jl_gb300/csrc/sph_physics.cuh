@@ -237,6 +237,7 @@ __device__ __forceinline__ void carry_frozen(int i, const SceneDev& S, const Sor
     const int32_t key = cell_key<DIM>(x, S);
     sc.key[i] = key;
     sc.slot[i] = atomicAdd(sc.count + key, 1);
+    count_tile(sc.tile_acc, key);
 }
 
 // ---------------------------------------------------------------- buffer neighbours

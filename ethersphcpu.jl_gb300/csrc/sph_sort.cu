@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t* __res
 // at most kScanDirectTiles tiles of kScanDirectItems x 256 cells (small tiles: many
 // blocks in flight on a small grid).  Block 0 also writes the total and advances the
 // steps.
-constexpr int kScanDirectItems = 4;
+constexpr int kScanDirectItems = kScanTileCells / kScanThreads;
 constexpr int kScanDirectTile = kScanThreads * kScanDirectItems;
 constexpr int kScanDirectTiles = 256;
 
@@ -245,8 +245,9 @@ __global__ void k_place(const SceneDev* __restrict__ scenes, SortedState src, Ne
     pdl_wait();
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    // count[] has been scanned: clear it for the next step's arrivals
+    // count[] and the tile sums have been scanned: clear them for the next step's arrivals
     for (int k = i; k < ncells; k += gridDim.x * blockDim.x) sc.count[k] = 0;
+    for (int k = i; k < ncells / kScanTileCells + 1; k += gridDim.x * blockDim.x) sc.block_sums[k] = 0;
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t key = sc.key[i];
     if (key == kDeadKey) return;
@@ -489,7 +490,11 @@ __global__ void __launch_bounds__(kScanTopThreads) k_scan_single(const int32_t* 
         for (int s = threadIdx.x; s < nscenes; s += blockDim.x) scene_step[s] += 1;
 }
 
-void launch_scan(const LaunchCtx& L, int advance) {
+bool scan_uses_tiles(int n) {
+    return n > kScanSingleChunks * kScanChunk && (n + kScanDirectTile - 1) / kScanDirectTile <= kScanDirectTiles;
+}
+
+void launch_scan(const LaunchCtx& L, int advance, bool tiles_ready) {
     const int n = L.total_cells;
     if (n <= kScanSingleChunks * kScanChunk) {
         launch_dep(k_scan_single, 1, kScanTopThreads, L.stream, L.sc.count, n, L.sc.start, L.n_next, L.sc.scene_step,
@@ -498,7 +503,8 @@ void launch_scan(const LaunchCtx& L, int advance) {
     }
     const int dtiles = (n + kScanDirectTile - 1) / kScanDirectTile;
     if (dtiles <= kScanDirectTiles) {
-        launch_dep(k_scan_tiles<kScanDirectItems>, dtiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums);
+        if (!tiles_ready)
+            launch_dep(k_scan_tiles<kScanDirectItems>, dtiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums);
         launch_dep(k_scan_down_direct, dtiles, kScanThreads, L.stream, L.sc.count, n, L.sc.block_sums, dtiles,
                    L.sc.start, L.n_next, L.sc.scene_step, L.nscenes, advance);
         return;
