@@ -28,7 +28,8 @@ module EtherSPHGPU
 using EtherSPHCPU
 
 export GPU, FP64, FP32Compensated, GPUScene, GPUBatch, SceneRequest, serve, step!, download!, probe, PlaneRules,
-       setBufferVelocity!
+    stepAsync!, synchronize, stats, countPairs, timeStages, autotune!, setLaunchShape!, setStencilPruning!, sceneInfo,
+    setBufferVelocity!
 
 const libsph = joinpath(@__DIR__, "..", "lib", "libethersph_gpu.so")
 
@@ -458,6 +459,89 @@ step!(s::GPUScene, first_step::Integer, nsteps::Integer) =
     checkStatus(s.h, ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), s.h, first_step, nsteps))
 download!(s::GPUScene, fluid) = downloadFluid!(s.h, fluid)
 
+"""
+    stepAsync!(s, first_step, nsteps); synchronize(s)
+
+sph_step_async / sph_synchronize: enqueue steps on the scene's stream and return at once;
+`synchronize` waits and reports a non-finite state or an overflow as an error.
+"""
+stepAsync!(s::GPUScene, first_step::Integer, nsteps::Integer) =
+    checkStatus(s.h, ccall((:sph_step_async, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), s.h, first_step, nsteps))
+synchronize(s::GPUScene) = checkStatus(s.h, ccall((:sph_synchronize, libsph), Int32, (Ptr{Cvoid},), s.h))
+
+# Mirror of SphStats (include/ethersph_gpu.h).
+struct SphStats
+    n_fluid::Int64
+    n_wall::Int64
+    steps_done::Int64
+    total_mass::Float64
+    kinetic_energy::Float64
+    max_speed::Float64
+    status_flags::Int32
+    reserved0::Int32
+end
+
+"""
+    stats(s) -> SphStats
+
+FP64 reductions on the device: live particles, total mass, kinetic energy, max speed.
+"""
+function stats(s::GPUScene)
+    out = Ref{SphStats}()
+    checkStatus(s.h, ccall((:sph_stats, libsph), Int32, (Ptr{Cvoid}, Ref{SphStats}), s.h, out))
+    return out[]
+end
+
+"""
+    countPairs(s) -> (fluid_pairs, wall_pairs)
+
+Unique fluid pairs (i < j, the CellListMap half-list convention) and fluid-wall pairs
+within r_cut at the current positions.
+"""
+function countPairs(s::GPUScene)
+    a, b = Ref{Int64}(0), Ref{Int64}(0)
+    checkStatus(s.h, ccall((:sph_count_pairs, libsph), Int32, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}), s.h, a, b))
+    return (a[], b[])
+end
+
+"""
+    timeStages(s; reps = 10) -> Vector{Float64}
+
+Milliseconds per stage (cell hash + count, scan, placement, continuity, momentum,
+Shepard), CUDA events on the scene's stream; the state is left unchanged.
+"""
+function timeStages(s::GPUScene; reps::Integer = 10)
+    ms = zeros(Float64, 6)
+    checkStatus(s.h, ccall((:sph_time_stages, libsph), Int32, (Ptr{Cvoid}, Int32, Ptr{Float64}), s.h, Int32(reps), ms))
+    return ms
+end
+
+"""
+    autotune!(s; reps = 3) -> NTuple{4, Int32}
+
+sph_autotune: the FP32-compensated form's launch shape picked on the scene's live state.
+"""
+function autotune!(s::GPUScene; reps::Integer = 3)
+    out = zeros(Int32, 4)
+    checkStatus(s.h, ccall((:sph_autotune, libsph), Int32, (Ptr{Cvoid}, Int32, Ptr{Int32}), s.h, Int32(reps), out))
+    return Tuple(out)
+end
+
+setLaunchShape!(s::GPUScene, shape::Vector{Int32}) =
+    checkStatus(s.h, ccall((:sph_set_launch_shape, libsph), Int32, (Ptr{Cvoid}, Ptr{Int32}), s.h, shape))
+setStencilPruning!(s::GPUScene, on::Bool) =
+    checkStatus(s.h, ccall((:sph_set_stencil_pruning, libsph), Int32, (Ptr{Cvoid}, Int32), s.h, Int32(on)))
+
+"""The cudaStream_t (as a pointer) the scene launches on, for CUDA-event timing."""
+function stream(s::GPUScene)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    checkStatus(s.h, ccall((:sph_get_stream, libsph), Int32, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), s.h, out))
+    return out[]
+end
+
+"""The library's ABI version (SPH_ABI_VERSION)."""
+abiVersion() = ccall((:sph_version, libsph), Int32, ())
+
 const probeCodes = Dict(:rho_ => 0, :p_ => 1, :c_ => 2, :t_ => 6, :mass_ => 7, "Density" => 0, "Pressure" => 1,
     "SoundSpeed" => 2, "VelocityX" => 3, "VelocityY" => 4, "VelocityZ" => 5, "Temperature" => 6, "Mass" => 7)
 
@@ -567,6 +651,18 @@ end
 stepBatch!(b::GPUBatch, nsteps::Integer) =
     checkStatus(b.h, ccall((:sph_batch_step, libsph), Int32, (Ptr{Cvoid}, Int64), b.h, nsteps))
 synchronize(b::GPUBatch) = checkStatus(b.h, ccall((:sph_synchronize, libsph), Int32, (Ptr{Cvoid},), b.h))
+
+"""
+    sceneInfo(b, id) -> (n_fluid, steps_done, finished, next_step)
+
+sph_batch_scene_info: the scene's live particles, steps run, whether its step budget is
+done, and the number of its next step.
+"""
+function sceneInfo(b::GPUBatch, id::Integer)
+    info = zeros(Int64, 4)
+    checkStatus(b.h, ccall((:sph_batch_scene_info, libsph), Int32, (Ptr{Cvoid}, Int32, Ptr{Int64}), b.h, Int32(id), info))
+    return (n_fluid = info[1], steps_done = info[2], finished = info[3] != 0, next_step = info[4])
+end
 retire!(b::GPUBatch, id::Integer) =
     checkStatus(b.h, ccall((:sph_batch_retire, libsph), Int32, (Ptr{Cvoid}, Int32), b.h, Int32(id)))
 
