@@ -174,10 +174,12 @@ def test_julia_binding_names_declared_entry_points_and_fields():
     assert called and called <= declared_symbols(), called - declared_symbols()
     assert {"sph_output_open", "sph_output_write", "sph_probe", "sph_batch_add_scene",
             "sph_scene_footprint"} <= called
-    body = re.search(r"struct SphParams\n(.*?)\nend", jl, flags=re.S).group(1)
-    jl_fields = re.findall(r"^\s*(\w+)::", body, flags=re.M)
     hdr = (ROOT / "include" / "ethersph_gpu.h").read_text()
-    c_body = re.search(r"typedef struct SphParams \{(.*?)\}\s*SphParams;", hdr, flags=re.S).group(1)
-    c_body = re.sub(r"/\*.*?\*/", "", c_body, flags=re.S)
-    c_fields = re.findall(r"\b(\w+)(?:\[\d\])?\s*;", c_body)
-    assert jl_fields == c_fields
+    for name in ("SphParams", "SphStats", "SphBufferRules"):  # mirrors: the C fields in order
+        m = re.search(r"struct %s\n(.*?)\nend" % name, jl, flags=re.S)
+        assert m, name
+        jl_fields = re.findall(r"^\s*(\w+)::", m.group(1), flags=re.M)
+        c_body = re.search(r"typedef struct %s \{(.*?)\}\s*%s;" % (name, name), hdr, flags=re.S).group(1)
+        c_body = re.sub(r"/\*.*?\*/", "", c_body, flags=re.S)
+        c_fields = re.findall(r"\b(\w+)(?:\[\d\])?\s*;", c_body)
+        assert jl_fields == c_fields, name
