@@ -42,7 +42,7 @@ LANES_LIST = 16  # SPH_LANES_LIST: momentum lanes codes >= 15 read the neighbour
 # bench's flushed steps), with the launch shape they were captured at
 DRAM_BYTES_256 = {
     "continuity": (3.839744e6, "-1,18,-1,128"),
-    "momentum": (15.297792e6, "-1,18,-1,128"),
+    "momentum": (15.29984e6, "-1,18,-1,128"),
 }
 
 
