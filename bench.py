@@ -49,7 +49,9 @@ DRAM_BYTES_256 = {
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    # 3,000 one-step graphs (each after an L2 flush) take about half a second: long
+    # enough for several clock samples at 100 ms inside the timed region
+    ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp64", "fp32c"], default="fp32c")
@@ -146,6 +148,10 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()  # the first sample marks a running sampler
+            while not self.samples and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
+            self.samples.clear()  # keep only samples taken during the timed region
         except FileNotFoundError:
             self.proc = None
         return self
