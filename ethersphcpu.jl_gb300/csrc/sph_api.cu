@@ -21,8 +21,20 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "sph_kernels.h"
 #include "sph_output.h"
+
+namespace {
+// NVTX range around a host entry point (shown by Nsight Systems; free without a tool).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+}  // namespace
 
 using namespace sph;
 
@@ -1180,6 +1192,7 @@ int32_t sph_create(const SphParams* params, int64_t fluid_capacity, int64_t wall
 int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double* v, const double* rho,
                          const double* p, const double* c, const double* mass, const double* gap, const double* t,
                          const double* kappa, const double* cp) {
+    NvtxRange nvtx_range("sph_upload_fluid");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles take fluid through sph_batch_add_scene");
     if (n < 0 || n > h->cap) return fail(h, SPH_ERR_GRID_OVERFLOW, "fluid count exceeds the handle capacity");
@@ -1205,6 +1218,7 @@ int32_t sph_upload_fluid(SphHandle* h, int64_t n, const double* x, const double*
 
 int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x, const double* normal,
                          const double* gap, const double* t, const double* kappa, const double* v) {
+    NvtxRange nvtx_range("sph_upload_walls");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles take walls through sph_batch_add_scene");
     SceneRec& R = h->scenes[0];
@@ -1216,6 +1230,7 @@ int32_t sph_upload_walls(SphHandle* h, int32_t kind, int64_t n, const double* x,
 }
 
 int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
+    NvtxRange nvtx_range("sph_step_async");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles step with sph_batch_step");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_step before sph_upload_fluid");
@@ -1240,6 +1255,7 @@ int32_t sph_step_async(SphHandle* h, int64_t first_step, int64_t nsteps) {
 }
 
 int32_t sph_synchronize(SphHandle* h) {
+    NvtxRange nvtx_range("sph_synchronize");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     cudaStream_t st = h->stream;
     SPH_CUDA(h, cudaMemcpyAsync(&h->h_pinned[1], h->sc.status, 4, cudaMemcpyDeviceToHost, st));
@@ -1264,6 +1280,7 @@ int32_t sph_step(SphHandle* h, int64_t first_step, int64_t nsteps) {
 
 int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, double* x, double* v, double* rho,
                            double* p, double* c, double* mass, double* gap, double* t, double* kappa, double* cp) {
+    NvtxRange nvtx_range("sph_download_fluid");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!n_out) return fail(h, SPH_ERR_ARG, "n_out is required");
     if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles download with sph_batch_download_scene");
@@ -1275,6 +1292,7 @@ int32_t sph_download_fluid(SphHandle* h, int64_t capacity, int64_t* n_out, doubl
 }
 
 int32_t sph_download_ids(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* ids_out) {
+    NvtxRange nvtx_range("sph_download_ids");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!n_out) return fail(h, SPH_ERR_ARG, "n_out is required");
     if (h->batch) return fail(h, SPH_ERR_STATE, "batch handles download with sph_batch_download_scene");
@@ -1327,6 +1345,7 @@ int32_t sph_batch_add_scene(SphHandle* h, const SphParams* params, int64_t first
                             const double* cp, int64_t n_wall, const int32_t* wall_kind, const double* wall_x,
                             const double* wall_normal, const double* wall_gap, const double* wall_t,
                             const double* wall_kappa, const double* wall_v, int32_t* scene_id) {
+    NvtxRange nvtx_range("sph_batch_add_scene");
     if (!h || !params || !scene_id) return fail(h, SPH_ERR_ARG, "null argument");
     if (!h->batch) return fail(h, SPH_ERR_STATE, "not a batch handle");
     if (!same_kind(h, *params)) return fail(h, SPH_ERR_ARG, "scene differs from the batch in dim/kernel/solve/form");
@@ -1369,6 +1388,7 @@ int32_t sph_batch_add_scene(SphHandle* h, const SphParams* params, int64_t first
 }
 
 int32_t sph_batch_step(SphHandle* h, int64_t nsteps) {
+    NvtxRange nvtx_range("sph_batch_step");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!h->batch) return fail(h, SPH_ERR_STATE, "not a batch handle");
     if (nsteps < 0) return fail(h, SPH_ERR_ARG, "negative step count");
@@ -1395,6 +1415,7 @@ int32_t sph_batch_scene_info(SphHandle* h, int32_t scene_id, int64_t* info) {
 int32_t sph_batch_download_scene(SphHandle* h, int32_t scene_id, int64_t capacity, int64_t* n_out, double* x,
                                  double* v, double* rho, double* p, double* c, double* mass, double* gap, double* t,
                                  double* kappa, double* cp) {
+    NvtxRange nvtx_range("sph_batch_download_scene");
     if (!h || !n_out) return fail(h, SPH_ERR_ARG, "null argument");
     if (scene_id < 0 || scene_id >= h->scap || !h->scenes[scene_id].used) return fail(h, SPH_ERR_ARG, "no such scene");
     return download_scene(h, scene_id, capacity, n_out, x, v, rho, p, c, mass, gap, t, kappa, cp, nullptr);
@@ -1558,6 +1579,7 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
 }
 
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
+    NvtxRange nvtx_range("sph_autotune");
     if (!h || reps < 1) return fail(h, SPH_ERR_ARG, "bad argument");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
     if (h->precision == SPH_PRECISION_FP32_COMPENSATED) {
@@ -1746,6 +1768,7 @@ int32_t sph_output_open(SphHandle* h, const char* dir_path, const char* file_nam
 }
 
 int32_t sph_output_write(SphHandle* h, int64_t file_step, double time) {
+    NvtxRange nvtx_range("sph_output_write");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (!h->out || !h->out->is_open()) return fail(h, SPH_ERR_STATE, "sph_output_write before sph_output_open");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_output_write before sph_upload_fluid");
@@ -1811,6 +1834,7 @@ int32_t sph_upload_buffers(SphHandle* h, const SphBufferRules* rules, int64_t ca
                            const double* mass, const double* gap, int64_t n_outlet, const double* ox,
                            const double* ov, const double* orho, const double* op, const double* oc,
                            const double* omass, const double* ogap) {
+    NvtxRange nvtx_range("sph_upload_buffers");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (h->batch) return fail(h, SPH_ERR_STATE, "inlet/outlet buffers are for single-scene handles");
     if (h->mode != 3) return fail(h, SPH_ERR_STATE, "buffers need solve = SPH_SOLVE_FLUID_INLET_OUTLET_WALL");
@@ -1964,6 +1988,7 @@ int32_t sph_download_buffers(SphHandle* h, int32_t which, int64_t capacity, int6
 
 int32_t sph_probe(SphHandle* h, int64_t n_points, const double* points, int32_t n_fields, const int32_t* fields,
                   double none_value, double* out) {
+    NvtxRange nvtx_range("sph_probe");
     if (!h) return fail(nullptr, SPH_ERR_ARG, "null handle");
     if (h->batch) return fail(h, SPH_ERR_STATE, "probes are for single-scene handles");
     if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "sph_probe before sph_upload_fluid");
