@@ -90,6 +90,10 @@ SIGNATURES = {
     "sph_download_ids": (C.c_int32, [_H, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_stats": (C.c_int32, [_H, C.POINTER(SphStats)]),
     "sph_count_pairs": (C.c_int32, [_H, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "sph_download_cell_keys": (C.c_int32, [_H, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int32)]),
+    "sph_download_neighbours": (C.c_int32, [_H, C.c_int64, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                            C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "sph_get_stream": (C.c_int32, [_H, C.POINTER(C.c_void_p)]),
     "sph_time_stages": (C.c_int32, [_H, C.c_int32, _DP]),
     "sph_output_open": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32,

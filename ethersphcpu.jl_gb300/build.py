@@ -57,7 +57,7 @@ def build(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIB_DIR.mkdir(exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), sources))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]

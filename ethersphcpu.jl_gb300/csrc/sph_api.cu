@@ -2,9 +2,9 @@
 //
 // One handle = one CUDA stream + the device state of one scene.  Step pipeline
 // (FluidWallSolve.jl:8-83 and its siblings), all on the handle's stream:
-//   memset(count) -> K4 continuity+EOS -> K5 momentum+integrate(+check, +next hash)
-//   -> [K6 Shepard] -> scan -> fill+place (stable (cell, id) reorder into the other
-//   buffer) -> swap.
+//   K4 continuity+EOS -> K5 momentum+integrate(+check, +next hash; on a re-initialisation
+//   step + the Shepard density) -> scan -> fill+place (stable (cell, id) reorder into the
+//   other buffer, count reset) -> swap.
 // Bundles of steps are captured once as CUDA graphs and replayed.
 //
 // Host arithmetic in this file (parameter constants, the EOS for uploads without
@@ -198,6 +198,16 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.inv_cp_f = (float)S.inv_cp_d;
     S.inv_rho0 = 1.0 / p.rho_0;
     S.inv_rho0_f = (float)(1.0 / p.rho_0);
+    S.b_f = (float)p.b;
+    S.p0_f = (float)p.p_0;
+    S.eos_poly = p.gamma >= 1 && p.gamma <= 8;
+    if (S.eos_poly) {  // C(gamma, k) = C(gamma, k - 1) (gamma - k + 1) / k, exact in FP32 here
+        double c = 1.0;
+        for (int k = 1; k <= p.gamma; ++k) {
+            c = c * (double)(p.gamma - k + 1) / (double)k;
+            S.eos_c[k - 1] = (float)c;
+        }
+    }
     return true;
 }
 
@@ -498,11 +508,12 @@ LaunchCtx make_ctx(SphHandle* h) {
     L.sc = h->sc;
     L.sc.n_live = h->nbuf + h->par;
     L.n_next = h->nbuf + (h->par ^ 1);
+    L.shepard = 0;
     L.force_reinit = 0;
+    L.skip_reinit = 0;
     L.block = h->tune[3];
     L.tpp_continuity = h->tune[0];
     L.tpp_momentum = h->tune[1];
-    L.tpp_reinit = h->tune[2];
     L.list_momentum = uses_list(h);
     if (L.list_momentum) L.tpp_momentum -= SPH_LANES_LIST;
     L.nl = h->nl;
@@ -526,7 +537,7 @@ void launch_physics(int stage, const LaunchCtx& L) {
 }
 
 // Enqueue one step (no synchronisation).  `reinit`: some running scene re-initialises
-// its density at this step (the kernel decides per scene).
+// its density at this step (the kernels decide per scene).
 void enqueue_step(SphHandle* h, bool reinit) {
     LaunchCtx L = make_ctx(h);
     // count[] and the tile sums were zeroed by the previous placement (or the last re-sort);
@@ -535,8 +546,18 @@ void enqueue_step(SphHandle* h, bool reinit) {
     const bool tiles = !h->has_buffers && scan_uses_tiles(L.total_cells);
     if (tiles) L.sc.tile_acc = h->sc.block_sums;
     launch_physics(0, L);
-    launch_physics(1, L);
-    if (reinit) launch_physics(2, L);
+    if (!reinit) {
+        launch_physics(1, L);
+    } else if (!h->batch) {  // the scene re-initialises: the momentum gather with the Shepard sums
+        L.shepard = 1;
+        launch_physics(1, L);
+    } else {  // each particle through the momentum gather of its own scene's step kind
+        L.skip_reinit = 1;
+        launch_physics(1, L);
+        L.shepard = 1;
+        L.skip_reinit = 0;
+        launch_physics(1, L);
+    }
     if (h->has_buffers) launch_buffers(L);  // before the scan advances the step counter
     launch_scan(L, 1, tiles);
     // fluid made from inlet particles has no FP32 shadows yet: convert everything then
@@ -1514,6 +1535,96 @@ int32_t sph_count_pairs(SphHandle* h, int64_t* fluid_pairs, int64_t* wall_pairs)
     return SPH_OK;
 }
 
+int32_t sph_download_cell_keys(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* keys, int32_t* grid) {
+    NvtxRange nvtx_range("sph_download_cell_keys");
+    if (!h || !n_out) return fail(h, SPH_ERR_ARG, "null argument");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "cell keys are for single-scene handles");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
+    const SceneDev& S = h->scenes[0].dev;
+    if (grid)
+        for (int a = 0; a < 3; ++a) grid[a] = S.n[a];
+    int32_t b = 0, e = 0;
+    if (int32_t rc = scene_range(h, 0, &b, &e); rc != SPH_OK) return rc;
+    const int64_t n = e - b;
+    *n_out = n;
+    if (!keys || n == 0) return SPH_OK;  // the count (and grid) only
+    if (n > capacity) return fail(h, SPH_ERR_ARG, "caller array too small for the live fluid");
+    cudaStream_t st = h->stream;
+    std::vector<int32_t> ids(n), hk(n), order;
+    int32_t* d_keys = nullptr;
+    SPH_CUDA(h, cudaMalloc((void**)&d_keys, (size_t)n * 4));
+    LaunchCtx L = make_ctx(h);
+    launch_cell_keys(L, b, e, d_keys);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hk.data(), d_keys, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(ids.data(), h->S[h->par].id + b, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cudaFree(d_keys);
+    if (err != cudaSuccess) return cuda_fail(h, err, "sph_download_cell_keys");
+    ascending_id_order(ids, order);
+    for (int64_t q = 0; q < n; ++q) keys[q] = hk[order[q]];
+    return SPH_OK;
+}
+
+int32_t sph_download_neighbours(SphHandle* h, int64_t capacity, int64_t ids_capacity, int64_t* n_out,
+                                int64_t* total_out, int64_t* offsets, int64_t* nbr_ids) {
+    NvtxRange nvtx_range("sph_download_neighbours");
+    if (!h || !n_out || !total_out || !offsets) return fail(h, SPH_ERR_ARG, "null argument");
+    if (h->batch) return fail(h, SPH_ERR_STATE, "neighbour lists are for single-scene handles");
+    if (!h->have_fluid) return fail(h, SPH_ERR_STATE, "no fluid uploaded");
+    int32_t b = 0, e = 0;
+    if (int32_t rc = scene_range(h, 0, &b, &e); rc != SPH_OK) return rc;
+    const int64_t n = e - b;
+    *n_out = n;
+    *total_out = 0;
+    if (n + 1 > capacity) return fail(h, SPH_ERR_ARG, "offsets array too small (live fluid + 1)");
+    offsets[0] = 0;
+    if (n == 0) return SPH_OK;
+    cudaStream_t st = h->stream;
+    LaunchCtx L = make_ctx(h);
+    std::vector<int32_t> ids(n), counts(n), order;
+    int32_t* d_counts = nullptr;
+    SPH_CUDA(h, cudaMalloc((void**)&d_counts, (size_t)n * 4));
+    launch_neighbours(L, b, e, d_counts, nullptr, nullptr);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaMemcpyAsync(counts.data(), d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(ids.data(), h->S[h->par].id + b, (size_t)n * 4, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    cudaFree(d_counts);
+    if (err != cudaSuccess) return cuda_fail(h, err, "sph_download_neighbours (counts)");
+    ascending_id_order(ids, order);
+    std::vector<int64_t> rows(n);  // first entry of each sorted particle's row
+    for (int64_t q = 0; q < n; ++q) {
+        rows[order[q]] = offsets[q];
+        offsets[q + 1] = offsets[q] + counts[order[q]];
+    }
+    const int64_t total = offsets[n];
+    *total_out = total;
+    if (!nbr_ids) return SPH_OK;
+    if (total > ids_capacity) return fail(h, SPH_ERR_ARG, "ids array too small for the neighbour lists");
+    if (total == 0) return SPH_OK;
+    int64_t* d_rows = nullptr;
+    int32_t* d_ids = nullptr;
+    std::vector<int32_t> hid(total);
+    err = cudaMalloc((void**)&d_rows, (size_t)n * 8);
+    if (err == cudaSuccess) err = cudaMalloc((void**)&d_ids, (size_t)total * 4);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d_rows, rows.data(), (size_t)n * 8, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) {
+        launch_neighbours(L, b, e, nullptr, d_rows, d_ids);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hid.data(), d_ids, (size_t)total * 4, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    if (d_rows) cudaFree(d_rows);
+    if (d_ids) cudaFree(d_ids);
+    if (err != cudaSuccess) return cuda_fail(h, err, "sph_download_neighbours (ids)");
+    for (int64_t q = 0; q < n; ++q) {
+        std::sort(hid.begin() + offsets[q], hid.begin() + offsets[q + 1]);
+        for (int64_t k = offsets[q]; k < offsets[q + 1]; ++k) nbr_ids[k] = hid[k];
+    }
+    return SPH_OK;
+}
+
 int32_t sph_get_stream(SphHandle* h, void** stream) {
     if (!h || !stream) return fail(h, SPH_ERR_ARG, "null argument");
     *stream = (void*)h->stream;
@@ -1535,8 +1646,10 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
     Lh.nx.v = L.st.v;
     Lh.nx.rho = L.st.rho;
     Lh.nx.T = L.st.T;
-    L.force_reinit = 1;
     L.bs.npend = nullptr;  // timed momentum launches mark no particle for the outlet
+    LaunchCtx Lr = L;      // the momentum gather of a re-initialisation step
+    Lr.shepard = 1;
+    Lr.force_reinit = 1;
     const int par = h->par;
     auto run = [&](int stage) {
         switch (stage) {
@@ -1548,10 +1661,12 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
             case SPH_STAGE_SORT: launch_place(Lh); break;
             case SPH_STAGE_CONTINUITY: launch_physics(0, L); break;
             case SPH_STAGE_MOMENTUM: launch_physics(1, L); break;
-            case SPH_STAGE_REINIT: launch_physics(2, L); break;
+            case SPH_STAGE_REINIT: launch_physics(1, Lr); break;
+            case SPH_NUM_STAGES: launch_physics(0, Lr); break;  // continuity forming the Shepard volumes
         }
     };
     for (int stage = 0; stage < SPH_NUM_STAGES; ++stage) {
+        if (stage == SPH_STAGE_REINIT) run(SPH_NUM_STAGES);
         run(stage);  // warm-up
         SPH_CUDA(h, cudaEventRecord(e0, st));
         for (int r = 0; r < reps; ++r) run(stage);
@@ -1605,10 +1720,9 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         // neighbour list / momentum reads it
         auto trial = [&](int stage, int tpp, int block, bool list) -> float {
             LaunchCtx L = make_ctx(h);
-            L.force_reinit = 1;
             L.bs.npend = nullptr;  // trial launches mark no particle for the outlet
             L.block = block;
-            L.tpp_continuity = L.tpp_momentum = L.tpp_reinit = tpp;
+            L.tpp_continuity = L.tpp_momentum = tpp;
             L.list_momentum = list ? 1 : 0;
             L.nl = h->nl;
             launch_physics(stage, L);  // warm-up
@@ -1637,7 +1751,6 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         const int walk_tpps[5] = {-1, 1, 2, 4, 8};  // -1: one lane, software-pipelined loop
         const Best c_walk = search(0, walk_tpps, 5, false);
         const Best m_walk = search(1, walk_tpps, 5, false);
-        const Best r_walk = search(2, walk_tpps, 5, false);
         Best c_list, m_list;
         if (have_list) {
             const int c_tpps[2] = {-1, 1}, m_tpps[4] = {-1, 1, 2, 4};
@@ -1650,7 +1763,6 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         // (continuity then momentum, at the momentum stage's block size)
         auto pair_ms = [&](const Best& c, const Best& m, bool list) -> float {
             LaunchCtx L = make_ctx(h);
-            L.force_reinit = 1;
             L.bs.npend = nullptr;
             L.block = m.block;
             L.tpp_continuity = c.tpp;
@@ -1683,7 +1795,6 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
             h->tune[1] = m_walk.tpp;
             h->tune[3] = m_walk.block;
         }
-        h->tune[2] = r_walk.tpp;
         if (!pick_list && h->nl.e) {  // the list storage of the trials is not needed
             SPH_CUDA(h, cudaStreamSynchronize(st));
             cudaFree(h->nl.e);

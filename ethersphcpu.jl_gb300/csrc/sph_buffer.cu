@@ -52,9 +52,7 @@ __global__ void k_buf_move(const SceneDev* __restrict__ scenes, BufferState cur,
                 st.gap[a] = cur.gap[b];
                 st.id[a] = (int32_t)(br.id_base + (step - br.first_step) * br.n_inlet + order);
                 st.scene[a] = 0;
-                const int32_t key = cell_key<DIM>(xo, S);
-                sc.key[a] = key;
-                sc.slot[a] = atomicAdd(sc.count + key, 1);
+                cell_arrival(sc, a, cell_key<DIM>(xo, S));
             } else {
                 atomicOr(sc.status, kStatusBufferOverflow);
             }

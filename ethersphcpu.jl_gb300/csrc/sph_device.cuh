@@ -11,6 +11,7 @@
 //   kappa, v, kind, wall_start[cells + 1]
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 #include <stdint.h>
@@ -86,7 +87,9 @@ struct SceneDev {
     float kw_a_f, kg_a_f, inv_h_f, c0_f, rho0_f, inv_cp_f, inv_rho0_f;
     float rc2_prune;    // rc2_f * (1 + 1e-5): conservative bound for the stencil pruning
     float inv_cell_fx;  // 1 / cell_f[0]
-    float pad_f;
+    float b_f, p0_f;
+    float eos_c[8];     // binomial coefficients C(gamma, k), k = 1..gamma (gamma <= 8)
+    int32_t eos_poly;   // 1: the FP32 equation of state runs on the binomial sum (1 <= gamma <= 8)
 };
 
 // ---------------------------------------------------------------- vector types
@@ -184,12 +187,24 @@ struct SortScratch {
 
 constexpr int32_t kScanTileCells = 1024;  // cells of a tile of the two-launch scan
 
-// Warp-aggregated count of arrivals per scan tile: lanes landing in one tile add once.
+// Warp-aggregated count of arrivals per scan tile: the lanes that reach this call
+// together (a coalesced group, whatever branch brought them here) are partitioned by
+// tile, and one lane per tile adds the partition's size.
 __device__ __forceinline__ void count_tile(int32_t* tile_acc, int32_t key) {
     if (!tile_acc) return;
     const int tile = key / kScanTileCells;
-    const unsigned peers = __match_any_sync(__activemask(), tile);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(tile_acc + tile, __popc(peers));
+    const cooperative_groups::coalesced_group here = cooperative_groups::coalesced_threads();
+    const cooperative_groups::coalesced_group peers = cooperative_groups::labeled_partition(here, tile);
+    if (peers.thread_rank() == 0) atomicAdd(tile_acc + tile, (int32_t)peers.size());
+}
+
+// A particle arrives in cell `key` for the next sort: its key, its arrival slot in the
+// cell and, when the step's scan reads tile sums (sc.tile_acc), its tile's count.  Every
+// site that adds to sc.count goes through here, so the tile sums can never miss one.
+__device__ __forceinline__ void cell_arrival(const SortScratch& sc, int32_t i, int32_t key) {
+    sc.key[i] = key;
+    sc.slot[i] = atomicAdd(sc.count + key, 1);
+    count_tile(sc.tile_acc, key);
 }
 
 // ---------------------------------------------------------------- inlet/outlet buffers

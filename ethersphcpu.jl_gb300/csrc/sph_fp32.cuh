@@ -19,6 +19,9 @@
 // neighbour loads).  With the neighbour-list shapes the continuity gather records each
 // particle's accepted neighbours (NbrList) and the momentum gather reads them instead of
 // walking the cells again; the walks may skip cells of a row beyond r_cut (row_span).
+// On a re-initialisation step the momentum gather also forms the Shepard sums over the
+// same neighbours (FP32 kernel values, FP64 sums) and writes the re-initialised density:
+// the update and the re-initialisation are one kernel.
 //
 // Same terms, order of walls after fluid, and solve variants as sph_fp64.cu; the
 // formulas follow Continuity.jl, PressureForce.jl, ViscosityForce.jl, WallForce.jl,
@@ -26,6 +29,7 @@
 #pragma once
 
 #include <climits>
+#include <type_traits>
 
 #include "sph_physics.cuh"
 #include "sph_kernels.h"
@@ -429,8 +433,10 @@ struct WallCand {
     float4 a, b, c;
     int kind;
 };
-struct CandShep {
-    float4 a;
+// A fluid candidate of the momentum gather on a re-initialisation step: the FP32
+// shadows plus the FP64 volume m/rho and mass of the Shepard sums.
+struct Cand3S {
+    float4 a, b, c;
     double vol, m;
 };
 
@@ -445,7 +451,7 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 // LIST (one lane per particle): also records the neighbours within r_cut in nl.
 template <int DIM, int KK, int TPP, bool PF, bool LIST>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
-                                 BufferState bf, NbrList nl) {
+                                 BufferState bf, NbrList nl, int force_reinit) {
     pdl_wait();
     static_assert(!LIST || TPP == 1, "the neighbour list is written by one lane per particle");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -486,8 +492,8 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
         const float d2 = dist2(rx, ry, rz);
-        if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
-        if (LIST) {
+        if (!(d2 <= S.rc2_f)) return;
+        if (LIST) {  // coincident neighbours are listed too: the Shepard sums count them
             if (cnt < nl.kmax) {
                 *lp = (int32_t)(((uint32_t)(j - i) << 9) | (uint32_t)code);
                 lp += nl.stride;
@@ -496,6 +502,7 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
             }
             ++cnt;
         }
+        if (d2 == 0.f) return;
         const float inv_r = rsqrtf(d2);
         const float r = d2 * inv_r;
         float W, dW;
@@ -525,32 +532,117 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         using V = typename VecT<DIM>::T;
         dr += buffer_drho<DIM, KK>(S, bf, c, ((const V*)st.x)[i], ((const V*)st.v)[i]);
     }
-    // Tait equation of state (UpdatePressure.jl:8-16) with one FP64 division and plain
-    // powers: FP64 is slow on GB300, and these values feed FP32 pair terms (P, c) or FP64
-    // sums (vol) where their last-bit differences from the reference's rounding do not show
+    // updateDensity! (UpdateDensity.jl:8-12) on the FP64 master density, then the Tait
+    // equation of state (UpdatePressure.jl:8-16) in FP32: its p, c and P feed FP32 pair
+    // terms, and FP64 work is slow on GB300.  It is evaluated on the relative change
+    // d = rho/rho0 - 1 (formed in FP64, then rounded), (1 + d)^gamma - 1 as the binomial
+    // sum of C(gamma, k) d^k by Horner, so no FP32 cancellation of (rho/rho0)^gamma - 1
+    // occurs; for gamma above 8 it runs in FP64.  The FP64 Shepard volume m/rho is formed
+    // only on the scene's re-initialisation steps (every step with force_reinit).
     // loads first: stores to the state arrays would otherwise order them (possible aliasing)
     double rho = st.rho[i];
-    const double m_i = st.m[i];
     const float4 fb_i = st.fb[i];
     const float4 fc_i = DIM == 3 ? st.fc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     rho += dr * S.dt;
-    const double inv_rho = 1.0 / rho;
-    const double rr = rho * S.inv_rho0;
-    const double p = S.b * (powi_plain(rr, S.gamma) - 1.0) + S.p0;
-    const double cs =
-        S.c0 * ((S.gamma & 1) ? powi_plain(rr, (S.gamma - 1) >> 1) : sqrt(powi_plain(rr, S.gamma - 1)));
-    const double P = p * inv_rho * inv_rho;
-    st.rhoc[i] = rho;
-    st.p[i] = p;
-    st.c[i] = cs;
-    st.P[i] = P;
-    st.vol[i] = m_i * inv_rho;
-    if (DIM == 2) {
-        st.fb[i] = make_float4(fb_i.x, (float)rho, (float)P, fb_i.w);
+    float p_f, c_f;
+    if (S.eos_poly) {
+        const float d = (float)((rho - S.rho0) * S.inv_rho0);
+        const int g = S.gamma;
+        float acc = S.eos_c[g - 1];
+        for (int k = g - 1; k >= 1; --k) acc = fmaf(acc, d, S.eos_c[k - 1]);
+        p_f = fmaf(S.b_f, acc * d, S.p0_f);
+        const float r1 = 1.f + d;
+        float rp = 1.f;  // (rho/rho0)^((gamma-1) div 2)
+        for (int k = 0; k < (g - 1) >> 1; ++k) rp *= r1;
+        c_f = S.c0_f * ((g & 1) ? rp : sqrtf(rp * rp * r1));
     } else {
-        st.fb[i] = make_float4(fb_i.x, fb_i.y, fb_i.z, (float)rho);
-        st.fc[i] = make_float4((float)P, fc_i.y, fc_i.z, fc_i.w);
+        const double rr = rho * S.inv_rho0;
+        p_f = (float)(S.b * (powi_plain(rr, S.gamma) - 1.0) + S.p0);
+        c_f = (float)(S.c0 * ((S.gamma & 1) ? powi_plain(rr, (S.gamma - 1) >> 1) : sqrt(powi_plain(rr, S.gamma - 1))));
     }
+    const float rho_f = (float)rho;
+    const float inv_rho_f = __frcp_rn(rho_f);
+    const float P = p_f * inv_rho_f * inv_rho_f;
+    st.rhoc[i] = rho;
+    st.p[i] = (double)p_f;
+    st.c[i] = (double)c_f;
+    st.P[i] = (double)P;
+    if (force_reinit || is_step(sc.scene_step[s], S.reinit_interval)) st.vol[i] = st.m[i] / rho;
+    if (DIM == 2) {
+        st.fb[i] = make_float4(fb_i.x, rho_f, P, fb_i.w);
+    } else {
+        st.fb[i] = make_float4(fb_i.x, fb_i.y, fb_i.z, rho_f);
+        st.fc[i] = make_float4(P, fc_i.y, fc_i.z, fc_i.w);
+    }
+}
+
+// -------------------------------------------------------------------- K5 epilogue, split
+// The forward-Euler update of K5 (UpdateTemperature/Velocity/Position.jl) with TPP >= DIM
+// lanes per particle, each lane holding the combined sums: lane k < DIM updates component
+// k of v and x on the FP64 masters, checks it (finite, inside the check box) and takes
+// its cell coordinate; lane 0 gathers those through the group and writes the scalars (T,
+// the density or its Shepard re-initialisation) and the arrival in the next cell list.
+// The same operations as the one-lane epilogue, spread over the components.
+template <int DIM, int MODE, int TPP, bool SHEP>
+__device__ __forceinline__ void momentum_epilogue_split(int i, int lane, const SceneDev& S, const SortedState& st,
+                                                        const NextState& nx, const SortScratch& sc,
+                                                        const Kahan (&dv)[3], const Kahan& dT, double sw, double sws) {
+    constexpr int VS = DIM == 2 ? 2 : 4;  // doubles per stored vector (double2 / double4)
+    const int k = lane;
+    if (k >= DIM) {
+        if (DIM == 3 && k == 3) {  // the unused w of the 3D vectors, as the one-lane epilogue writes it
+            ((double*)nx.x)[(int64_t)i * VS + 3] = 0.0;
+            ((double*)nx.v)[(int64_t)i * VS + 3] = 0.0;
+        }
+        return;
+    }
+    const int base = (int)(threadIdx.x & 31u) & ~(TPP - 1);
+    const unsigned cmask = ((1u << DIM) - 1u) << base;
+    const int64_t step = sc.scene_step[st.scene[i]];
+    // loads first: the stores below would otherwise order them (possible aliasing)
+    const double x0 = ((const double*)st.x)[(int64_t)i * VS + k];
+    const double v0 = ((const double*)st.v)[(int64_t)i * VS + k];
+    const double rho_d = st.rhoc[i];
+    const double T0 = MODE == kModeThermal ? st.T[i] : 0.0;
+    const double dvd = (k == 0 ? dv[0] : (k == 1 ? dv[1] : dv[DIM - 1])).value();
+    const double dt = S.dt;
+    double Tn = 0.0, body;
+    if (MODE == kModeThermal) {  // every component lane forms the same temperature
+        Tn = T0 + dt * dT.value();
+        body = S.bous[k] * (Tn - S.t0);
+    } else {
+        body = S.g[k];
+    }
+    double vn = v0, xn = x0;
+    vn += body * dt;
+    vn += dvd * dt;
+    xn += vn * dt - dvd * S.half_dtdt;  // dv dt^2 / 2
+    if (k == 0 && S.periodic_x) {
+        if (xn >= S.wrap_hi) xn -= S.period;
+        else if (xn < S.lo[0]) xn += S.period;
+    }
+    ((double*)nx.x)[(int64_t)i * VS + k] = xn;
+    ((double*)nx.v)[(int64_t)i * VS + k] = vn;
+    const bool bad = !(bits_finite(xn) & bits_finite(vn));
+    const bool out = S.check_enabled && is_step(step, S.check_interval) && ((xn > S.check_hi[k]) | (xn < S.check_lo[k]));
+    const int32_t ck = cell_coord(xn, S, k);
+    const unsigned bad_lanes = __ballot_sync(cmask, bad) & cmask;
+    const unsigned out_lanes = __ballot_sync(cmask, out) & cmask;
+    const int32_t cy = __shfl_sync(cmask, ck, base + 1);
+    const int32_t cz = DIM == 3 ? __shfl_sync(cmask, ck, base + DIM - 1) : 0;
+    if (k != 0) return;
+    if (MODE == kModeThermal) nx.T[i] = Tn;
+    else if (nx.T) nx.T[i] = st.T[i];
+    double rho_out = rho_d;
+    if constexpr (SHEP) {  // the particle's own W(0) term (ReconstructValue.jl:51-55), then the quotient
+        sw += S.k0 * st.vol[i];
+        sws += S.k0 * st.m[i];
+        rho_out = sws / sw;
+    }
+    nx.rho[i] = rho_out;
+    if ((bad_lanes || !bits_finite(rho_d)) && S.nan_check) atomicOr(sc.status, kStatusNonFinite);
+    if (out_lanes) sc.key[i] = kDeadKey;
+    else cell_arrival(sc, i, S.cell_off + (cz * S.n[1] + cy) * S.n[0] + ck);
 }
 
 // -------------------------------------------------------------------- K5 (FP32)
@@ -561,10 +653,18 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
 // prefetched candidate would spill) and is therefore limited to blocks of 256 threads.
 // LIST: the fluid neighbours come from the list the continuity gather recorded (the
 // cell walk for a particle whose list did not fit).
-template <int DIM, int KK, int MODE, int TPP, bool PF, bool LIST>
+// SHEP: the momentum gather of density re-initialisation steps.  It takes the particles
+// of the scenes whose step re-initialises (every running scene when `sel` is set): the
+// fluid walk also sums W m_j/rho_j and W m_j (ReconstructValue.jl:28-50) in FP64, and the
+// particle's density leaves the step as the Shepard quotient instead of the continuity
+// update.  Without SHEP, `sel` set leaves those particles to the SHEP launch of the same
+// step (a batch whose scenes re-initialise at different steps runs both): every particle
+// goes through the kernel of its own scene's step kind, so a scene's result does not
+// depend on the other scenes of its batch.
+template <int DIM, int KK, int MODE, int TPP, bool PF, bool LIST, bool SHEP>
 __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, WallState wl,
                                SortScratch sc, int32_t cap, BufferState bf, BufferScratch bs, BufferRules br,
-                               NbrList nl) {
+                               NbrList nl, int sel) {
     pdl_wait();
     using V = typename VecT<DIM>::T;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -572,7 +672,15 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
-    if (!scene_runs(S, sc.scene_step[s])) {
+    const int64_t step_s = sc.scene_step[s];
+    const bool runs = scene_runs(S, step_s);
+    const bool reinit_scene = runs && is_step(step_s, S.reinit_interval);
+    if constexpr (SHEP) {
+        if (!(runs && (sel || reinit_scene))) return;
+    } else {
+        if (sel && reinit_scene) return;
+    }
+    if (!runs) {
         if (lane == 0) carry_frozen<DIM>(i, S, st, nx, sc);
         return;
     }
@@ -605,17 +713,23 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     int32_t c[3];
     decode_cell(st.cell[i], S, c);
     Kahan dv[3], dT;
+    double sw = 0.0, sws = 0.0;  // Shepard sums (FP64)
 
     // every load of a candidate is issued before its distance test (one memory round
     // trip per candidate), and before the previous candidate is processed
+    using CandF = std::conditional_t<SHEP, Cand3S, Cand3>;
     auto load_f = [&](int j) {
-        Cand3 d;
+        CandF d;
         d.a = st.fa[j];
         d.b = st.fb[j];
         d.c = (DIM == 3 || MODE == kModeThermal) ? st.fc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (SHEP) {
+            d.vol = st.vol[j];
+            d.m = st.m[j];
+        }
         return d;
     };
-    auto pair = [&](int j, const Cand3& cd, float ox, float oy, float oz, int) {
+    auto pair = [&](int j, const CandF& cd, float ox, float oy, float oz, int) {
         if (j == i) return;
         const float4 aj = cd.a;
         const float4 bj = cd.b;
@@ -623,11 +737,23 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         const float rx = xi[0] - ox - aj.x, ry = xi[1] - oy - aj.y;
         const float rz = DIM == 3 ? xi[2] - oz - aj.z : 0.f;
         const float d2 = dist2(rx, ry, rz);
-        if (!(d2 <= S.rc2_f) || d2 == 0.f) return;
+        if (!(d2 <= S.rc2_f)) return;
+        if (d2 == 0.f) {  // a coincident neighbour: no force, W(0) in the Shepard sums
+            if constexpr (SHEP) {
+                const double W0 = (double)kernel_w_f<KK>(0.f, S);
+                sw += W0 * cd.vol;
+                sws += W0 * cd.m;
+            }
+            return;
+        }
         const float inv_r = rsqrtf(d2);
         const float r = d2 * inv_r;
         float W, dW;
         kernel_wdw_f<KK>(r * inv_h, S, W, dW);
+        if constexpr (SHEP) {
+            sw += (double)W * cd.vol;
+            sws += (double)W * cd.m;
+        }
         float vx, vy, vz, m_j, rho_j, P_j, gap_j;
         float T_j = 0.f, kap_j = 0.f;
         if (DIM == 2) {
@@ -758,6 +884,18 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
 #pragma unroll
     for (int k = 0; k < DIM; ++k) group_combine<TPP>(dv[k], mask);
     if (MODE == kModeThermal) group_combine<TPP>(dT, mask);
+    if constexpr (SHEP) {
+        sw = group_sum<TPP>(sw, mask);
+        sws = group_sum<TPP>(sws, mask);
+    }
+    if constexpr (TPP >= DIM && MODE != kModeBuffers) {
+        // Every lane of the group holds the combined sums: lane k integrates component k in
+        // FP64 and hashes its cell coordinate, so the FP64 work of a particle (GB300's
+        // FP64 pipe is narrow) is spread over DIM lanes instead of left to lane 0 of a
+        // half-idle warp; lane 0 then adds the scalars and the cell arrival.
+        momentum_epilogue_split<DIM, MODE, TPP, SHEP>(i, lane, S, st, nx, sc, dv, dT, sw, sws);
+        return;
+    }
     if (lane != 0) return;
     double dvd[DIM];
 #pragma unroll
@@ -769,6 +907,10 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     const V x0 = ((const V*)st.x)[i];
     const V v0 = ((const V*)st.v)[i];
     const double rho_d = st.rhoc[i];  // loaded before the stores below (possible aliasing)
+    if constexpr (SHEP) {  // the particle's own W(0) term (ReconstructValue.jl:51-55)
+        sw += S.k0 * st.vol[i];
+        sws += S.k0 * st.m[i];
+    }
     if (MODE == kModeBuffers && bf.n) {  // inlet/outlet buffer neighbours, FP64
         const double gap_d = st.gap[i];
         buffer_dv<DIM, KK>(S, bf, c, x0, v0, rho_d, st.P[i], gap_d, kernel_w<KK>(gap_d, S), S.nu0 * rho_d, dvd);
@@ -811,7 +953,7 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
     }
     ((V*)nx.x)[i] = xo;
     ((V*)nx.v)[i] = vo;
-    nx.rho[i] = rho_d;
+    nx.rho[i] = SHEP ? sws / sw : rho_d;
 
     bool finite = bits_finite(rho_d);
 #pragma unroll
@@ -831,78 +973,35 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         if (k < bs.cap) bs.pend[k] = i;
         else atomicOr(sc.status, kStatusBufferOverflow);
     } else {
-        const int32_t key = cell_key<DIM>(xo, S);
-        sc.key[i] = key;
-        sc.slot[i] = atomicAdd(sc.count + key, 1);
-        count_tile(sc.tile_acc, key);
+        cell_arrival(sc, i, cell_key<DIM>(xo, S));
     }
 }
 
-// -------------------------------------------------------------------- K6 (FP32 W, FP64 sums)
-template <int DIM, int KK, int TPP, bool PF>
-__global__ void k_reinit_f32(const SceneDev* __restrict__ scenes, SortedState st, NextState nx, SortScratch sc,
-                             int32_t cap, int force) {
-    pdl_wait();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = t / TPP, lane = t % TPP;
-    if (i >= cap || i >= *sc.n_live) return;
-    const int32_t s = st.scene[i];
-    const SceneDev& S = scenes[s];
-    const int64_t step_s = sc.scene_step[s];
-    if (!scene_runs(S, step_s) || (!force && !is_step(step_s, S.reinit_interval))) return;
-    const float4 ai = st.fa[i];
-    const float xi0 = ai.x, xi1 = ai.y, xi2 = DIM == 3 ? ai.z : 0.f;
-    int32_t c[3];
-    decode_cell(st.cell[i], S, c);
-    double sw = 0.0, sws = 0.0;
-    auto load = [&](int j) { return CandShep{st.fa[j], st.vol[j], st.m[j]}; };
-    const float xs[3] = {xi0, xi1, xi2};
-    walk<DIM, TPP, PF>(S, sc.start, c, xs, lane, load, [&](int j, const CandShep& cd, float ox, float oy,
-                                                            float oz, int) {
-        if (j == i) return;
-        const float4 aj = cd.a;
-        const float rx = xi0 - ox - aj.x, ry = xi1 - oy - aj.y;
-        const float rz = DIM == 3 ? xi2 - oz - aj.z : 0.f;
-        const float d2 = dist2(rx, ry, rz);
-        if (!(d2 <= S.rc2_f)) return;
-        const double W = (double)kernel_w_f<KK>(sqrtf(d2) * S.inv_h_f, S);
-        sw += W * cd.vol;
-        sws += W * cd.m;
-    });
-    const unsigned mask = group_mask<TPP>();
-    sw = group_sum<TPP>(sw, mask);
-    sws = group_sum<TPP>(sws, mask);
-    if (lane != 0) return;
-    sw += S.k0 * st.vol[i];
-    sws += S.k0 * st.m[i];
-    nx.rho[i] = sws / sw;
+// -------------------------------------------------------------------- launchers
+// SHEP selects the momentum gather of re-initialisation steps; its instantiations live in
+// translation units of their own (the *_shep.cu files), so the two sets compile in parallel.
+template <int DIM, int KK, int MODE, int TPP, bool PF, bool LIST, bool SHEP>
+void launch_momentum(const LaunchCtx& L, int grid, int block) {
+    launch_dep(k_momentum_f32<DIM, KK, MODE, TPP, PF, LIST, SHEP>, grid, block, L.stream, L.scenes, L.st, L.nx, L.wl,
+               L.sc, L.cap, L.bf, L.bs, L.br, L.nl, SHEP ? L.force_reinit : L.skip_reinit);
 }
 
-// -------------------------------------------------------------------- launchers
-template <int DIM, int KK, int TPP, bool PF, bool LIST>
+template <int DIM, int KK, int TPP, bool PF, bool LIST, bool SHEP>
 void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        if constexpr (!LIST || TPP == 1)
+        if constexpr (!SHEP && (!LIST || TPP == 1))
             launch_dep(k_continuity_f32<DIM, KK, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.sc, L.cap,
-                       L.bf, L.nl);
-    } else if (stage == 2) {
-        if constexpr (!LIST)
-            launch_dep(k_reinit_f32<DIM, KK, TPP, PF>, grid, block, L.stream, L.scenes, L.st, L.nx, L.sc, L.cap,
-                       L.force_reinit);
+                       L.bf, L.nl, L.force_reinit);
     } else if (mode == kModeFluidWall) {
-        launch_dep(k_momentum_f32<DIM, KK, kModeFluidWall, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
-                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_momentum<DIM, KK, kModeFluidWall, TPP, PF, LIST, SHEP>(L, grid, block);
     } else if (mode == kModeWallPressure) {
-        launch_dep(k_momentum_f32<DIM, KK, kModeWallPressure, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st,
-                   L.nx, L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_momentum<DIM, KK, kModeWallPressure, TPP, PF, LIST, SHEP>(L, grid, block);
     } else if (mode == kModeBuffers) {
-        launch_dep(k_momentum_f32<DIM, KK, kModeBuffers, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
-                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_momentum<DIM, KK, kModeBuffers, TPP, PF, LIST, SHEP>(L, grid, block);
     } else {
-        launch_dep(k_momentum_f32<DIM, KK, kModeThermal, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.nx,
-                   L.wl, L.sc, L.cap, L.bf, L.bs, L.br, L.nl);
+        launch_momentum<DIM, KK, kModeThermal, TPP, PF, LIST, SHEP>(L, grid, block);
     }
 }
 
@@ -910,39 +1009,39 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
 // candidate loop (pays off when few warps are resident, i.e. small scenes).  The cell
 // walks (LIST false) take every code for every stage; with the neighbour list (LIST
 // true) continuity runs one lane (1 or -1) and momentum 1, 2, 4 or -1 lanes.
-template <int DIM, int KK, bool LIST>
+template <int DIM, int KK, bool LIST, bool SHEP>
 void launch_kk(int stage, const LaunchCtx& L) {
-    const int tpp = stage == 0 ? L.tpp_continuity : (stage == 1 ? L.tpp_momentum : L.tpp_reinit);
+    const int tpp = stage == 0 ? L.tpp_continuity : L.tpp_momentum;
     if constexpr (LIST) {
         if (stage == 0) {
-            if (tpp == -1) launch_tpp<DIM, KK, 1, true, true>(stage, L.mode, L);
-            else launch_tpp<DIM, KK, 1, false, true>(stage, L.mode, L);
+            if (tpp == -1) launch_tpp<DIM, KK, 1, true, true, SHEP>(stage, L.mode, L);
+            else launch_tpp<DIM, KK, 1, false, true, SHEP>(stage, L.mode, L);
             return;
         }
         switch (tpp) {
-            case -1: launch_tpp<DIM, KK, 1, true, true>(stage, L.mode, L); break;
-            case 1: launch_tpp<DIM, KK, 1, false, true>(stage, L.mode, L); break;
-            case 2: launch_tpp<DIM, KK, 2, false, true>(stage, L.mode, L); break;
-            default: launch_tpp<DIM, KK, 4, false, true>(stage, L.mode, L); break;
+            case -1: launch_tpp<DIM, KK, 1, true, true, SHEP>(stage, L.mode, L); break;
+            case 1: launch_tpp<DIM, KK, 1, false, true, SHEP>(stage, L.mode, L); break;
+            case 2: launch_tpp<DIM, KK, 2, false, true, SHEP>(stage, L.mode, L); break;
+            default: launch_tpp<DIM, KK, 4, false, true, SHEP>(stage, L.mode, L); break;
         }
     } else {
         switch (tpp) {
-            case -1: launch_tpp<DIM, KK, 1, true, false>(stage, L.mode, L); break;
-            case 1: launch_tpp<DIM, KK, 1, false, false>(stage, L.mode, L); break;
-            case 2: launch_tpp<DIM, KK, 2, false, false>(stage, L.mode, L); break;
-            case 8: launch_tpp<DIM, KK, 8, false, false>(stage, L.mode, L); break;
-            default: launch_tpp<DIM, KK, 4, false, false>(stage, L.mode, L); break;
+            case -1: launch_tpp<DIM, KK, 1, true, false, SHEP>(stage, L.mode, L); break;
+            case 1: launch_tpp<DIM, KK, 1, false, false, SHEP>(stage, L.mode, L); break;
+            case 2: launch_tpp<DIM, KK, 2, false, false, SHEP>(stage, L.mode, L); break;
+            case 8: launch_tpp<DIM, KK, 8, false, false, SHEP>(stage, L.mode, L); break;
+            default: launch_tpp<DIM, KK, 4, false, false, SHEP>(stage, L.mode, L); break;
         }
     }
 }
 
-template <int DIM, bool LIST>
+template <int DIM, bool LIST, bool SHEP>
 void dispatch(int stage, const LaunchCtx& L) {
     switch (L.kernel) {
-        case SPH_KERNEL_CUBIC_SPLINE: launch_kk<DIM, SPH_KERNEL_CUBIC_SPLINE, LIST>(stage, L); break;
-        case SPH_KERNEL_GAUSSIAN: launch_kk<DIM, SPH_KERNEL_GAUSSIAN, LIST>(stage, L); break;
-        case SPH_KERNEL_WENDLAND_C2: launch_kk<DIM, SPH_KERNEL_WENDLAND_C2, LIST>(stage, L); break;
-        default: launch_kk<DIM, SPH_KERNEL_WENDLAND_C4, LIST>(stage, L); break;
+        case SPH_KERNEL_CUBIC_SPLINE: launch_kk<DIM, SPH_KERNEL_CUBIC_SPLINE, LIST, SHEP>(stage, L); break;
+        case SPH_KERNEL_GAUSSIAN: launch_kk<DIM, SPH_KERNEL_GAUSSIAN, LIST, SHEP>(stage, L); break;
+        case SPH_KERNEL_WENDLAND_C2: launch_kk<DIM, SPH_KERNEL_WENDLAND_C2, LIST, SHEP>(stage, L); break;
+        default: launch_kk<DIM, SPH_KERNEL_WENDLAND_C4, LIST, SHEP>(stage, L); break;
     }
 }
 

@@ -4,6 +4,6 @@
 
 namespace sph {
 
-void launch_physics_fp32_3d(int stage, const LaunchCtx& L) { dispatch<3, false>(stage, L); }
+void launch_physics_fp32_3d(int stage, const LaunchCtx& L) { dispatch<3, false, false>(stage, L); }
 
 }  // namespace sph

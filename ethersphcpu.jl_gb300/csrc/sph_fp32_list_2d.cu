@@ -5,6 +5,6 @@
 
 namespace sph {
 
-void launch_physics_fp32_list_2d(int stage, const LaunchCtx& L) { dispatch<2, true>(stage, L); }
+void launch_physics_fp32_list_2d(int stage, const LaunchCtx& L) { dispatch<2, true, false>(stage, L); }
 
 }  // namespace sph

@@ -4,6 +4,6 @@
 
 namespace sph {
 
-void launch_physics_fp32_list_3d(int stage, const LaunchCtx& L) { dispatch<3, true>(stage, L); }
+void launch_physics_fp32_list_3d(int stage, const LaunchCtx& L) { dispatch<3, true, false>(stage, L); }
 
 }  // namespace sph

@@ -1,0 +1,9 @@
+// sph_fp32_list_3d_shep.cu — the FP32-compensated momentum gather of density re-initialisation steps
+// (momentum with the Shepard sums, sph_fp32.cuh) for 3D scenes with neighbour-list walks.
+#include "sph_fp32.cuh"
+
+namespace sph {
+
+void launch_momentum_fp32_list_3d_shep(const LaunchCtx& L) { dispatch<3, true, true>(1, L); }
+
+}  // namespace sph

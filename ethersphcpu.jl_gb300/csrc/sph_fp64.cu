@@ -6,7 +6,10 @@
 //    updateVelocity! + updatePosition!, fused with the out-of-domain check and the
 //    cell hash of the next step's sort   (PressureForce.jl, ViscosityForce.jl,
 //    WallForce.jl, ThermalConduction.jl, SelfAction/*.jl, FluidWallSolve.jl:37-81)
-// K6 Shepard density re-initialisation  (ReconstructValue.jl:22-57)
+// On a re-initialisation step K5 also forms the Shepard sums of reconstructScalar!
+//    (ReconstructValue.jl:22-57) over the same fluid neighbours, in the same order, at
+//    the same start-of-step positions, and writes the re-initialised density: the update
+//    and the re-initialisation are one kernel (FluidWallSolve.jl:64-72).
 //
 // One thread per fluid particle in sorted (cell, id) order; each thread sums its own
 // full neighbour list in a fixed order (cells z, y, x; particles by id), so there are
@@ -95,18 +98,25 @@ __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restr
     st.P[i] = p / (rho * rho);
 }
 
-template <int DIM, int KK, int MODE>
+// SHEP: the momentum gather of density re-initialisation steps, for the particles of the
+// scenes whose step re-initialises (every running scene when `sel` is set).  Without SHEP,
+// `sel` set leaves those particles to the SHEP launch of the same step (a batch whose
+// scenes re-initialise at different steps runs both).
+template <int DIM, int KK, int MODE, bool SHEP>
 __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restrict__ scenes, SortedState st,
                                                        NextState nx, WallState wl, SortScratch sc,
                                                        int32_t cap, BufferState bf, BufferScratch bs,
-                                                       BufferRules br) {
+                                                       BufferRules br, int sel) {
     using V = typename VecT<DIM>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cap || i >= *sc.n_live) return;
     const int32_t s = st.scene[i];
     const SceneDev& S = scenes[s];
     const int64_t step = sc.scene_step[s];
-    if (!scene_runs(S, step)) {
+    const bool runs = scene_runs(S, step);
+    const bool reinit_scene = runs && is_step(step, S.reinit_interval);
+    if (SHEP ? !(runs && (sel || reinit_scene)) : (sel && reinit_scene)) return;
+    if (!runs) {
         carry_frozen<DIM>(i, S, st, nx, sc);
         return;
     }
@@ -134,6 +144,9 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
 #pragma unroll
     for (int k = 0; k < DIM; ++k) dv[k] = 0.0;
     double dT = 0.0;
+    // Shepard sums (ReconstructValue.jl:28-50): sum W m_j/rho_j and sum W m_j/rho_j rho_j
+    // over the fluid neighbours, with the post-continuity densities
+    double sw = 0.0, sws = 0.0;
 
     // ---- fluid neighbours: pressureForce! + viscosityForce! (+ thermalConduction!)
     walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
@@ -156,6 +169,10 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
             if (DIM == 3) vv[DIM - 1] = comp(vi, DIM - 1) - comp(vj, DIM - 1);
             const double rho_j = st.rhoc[j];
             const double m_j = st.m[j];
+            if (SHEP) {
+                sw += W * m_j / rho_j;
+                sws += W * m_j / rho_j * rho_j;
+            }
             // PressureForce.jl:14-19
             double prho2 = P_i + st.P[j];
             const double Wg = S.uniform_gap ? Wg_i : kernel_w<KK>((gap_i + st.gap[j]) / 2.0, S);
@@ -330,7 +347,13 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
     }
     ((V*)nx.x)[i] = xo;
     ((V*)nx.v)[i] = vo;
-    nx.rho[i] = rho_i;
+    if (SHEP) {  // the particle's own W(0) term, then the Shepard quotient
+        sw += S.k0 * m_i / rho_i;
+        sws += S.k0 * m_i / rho_i * rho_i;
+        nx.rho[i] = sws / sw;
+    } else {
+        nx.rho[i] = rho_i;
+    }
 
     // ---- non-finite state, out-of-domain check, next step's cell hash
     bool finite = isfinite(rho_i);
@@ -351,45 +374,8 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
         if (k < bs.cap) bs.pend[k] = i;
         else atomicOr(sc.status, kStatusBufferOverflow);
     } else {
-        const int32_t key = cell_key<DIM>(xo, S);
-        sc.key[i] = key;
-        sc.slot[i] = atomicAdd(sc.count + key, 1);
-        count_tile(sc.tile_acc, key);
+        cell_arrival(sc, i, cell_key<DIM>(xo, S));
     }
-}
-
-template <int DIM, int KK>
-__global__ void __launch_bounds__(128) k_reinit_fp64(const SceneDev* __restrict__ scenes, SortedState st,
-                                                     NextState nx, SortScratch sc, int32_t cap, int force) {
-    using V = typename VecT<DIM>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cap || i >= *sc.n_live) return;
-    const int32_t s = st.scene[i];
-    const SceneDev& S = scenes[s];
-    const int64_t step = sc.scene_step[s];
-    if (!scene_runs(S, step) || (!force && !is_step(step, S.reinit_interval))) return;
-    const V* __restrict__ x = (const V*)st.x;
-    const V xi = x[i];
-    int32_t c[3];
-    cell_of<DIM>(xi, S, c);
-    double sw = 0.0, sws = 0.0;
-    walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
-        for (int j = jb; j < je; ++j) {
-            if (j == i) continue;
-            double rv[DIM];
-            make_rvec<DIM>(xi, x[j], S, rv);
-            const double d2 = norm_sq<DIM>(rv);
-            if (!(d2 <= S.rc2)) continue;
-            const double W = kernel_w<KK>(sqrt(d2), S);
-            const double m_j = st.m[j], rho_j = st.rhoc[j];
-            sw += W * m_j / rho_j;
-            sws += W * m_j / rho_j * rho_j;
-        }
-    });
-    const double m_i = st.m[i], rho_i = st.rhoc[i];
-    sw += S.k0 * m_i / rho_i;
-    sws += S.k0 * m_i / rho_i * rho_i;
-    nx.rho[i] = sws / sw;
 }
 
 // ---------------------------------------------------------------- launchers
@@ -402,13 +388,12 @@ void launch_k4(const LaunchCtx& L) {
 template <int DIM, int KK, int MODE>
 void launch_k5(const LaunchCtx& L) {
     const int grid = (L.cap + 127) / 128;
-    k_momentum_fp64<DIM, KK, MODE><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap, L.bf, L.bs,
-                                                                 L.br);
-}
-template <int DIM, int KK>
-void launch_k6(const LaunchCtx& L) {
-    const int grid = (L.cap + 127) / 128;
-    k_reinit_fp64<DIM, KK><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.sc, L.cap, L.force_reinit);
+    if (L.shepard)
+        k_momentum_fp64<DIM, KK, MODE, true><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap,
+                                                                          L.bf, L.bs, L.br, L.force_reinit);
+    else
+        k_momentum_fp64<DIM, KK, MODE, false><<<grid, 128, 0, L.stream>>>(L.scenes, L.st, L.nx, L.wl, L.sc, L.cap,
+                                                                           L.bf, L.bs, L.br, L.skip_reinit);
 }
 
 template <int DIM>
@@ -416,7 +401,6 @@ void dispatch_kk(int kk, int stage, int mode, const LaunchCtx& L) {
 #define SPH_KK_CASE(KKV)                                                        \
     case KKV:                                                                   \
         if (stage == 0) launch_k4<DIM, KKV>(L);                                 \
-        else if (stage == 2) launch_k6<DIM, KKV>(L);                            \
         else if (mode == kModeFluidWall) launch_k5<DIM, KKV, kModeFluidWall>(L); \
         else if (mode == kModeWallPressure) launch_k5<DIM, KKV, kModeWallPressure>(L); \
         else if (mode == kModeBuffers) launch_k5<DIM, KKV, kModeBuffers>(L);    \

@@ -26,10 +26,17 @@ struct LaunchCtx {
     WallState wl;
     SortScratch sc;
     int32_t* n_next;  // live count after the sort being built
-    int force_reinit; // 1: re-initialise every scene regardless of its step (stage timing)
+    // shepard = 1: the momentum launch of re-initialisation steps (it also forms the Shepard
+    // sums and writes the re-initialised density), for the particles of the scenes whose
+    // step re-initialises; force_reinit = 1 with it: of every running scene, whatever its
+    // step (stage timing).  skip_reinit = 1 with shepard = 0: the ordinary momentum launch
+    // leaves those particles to the shepard launch of the same step.
+    int shepard;
+    int force_reinit;
+    int skip_reinit;
     // launch shape of the FP32 gathers (lanes per particle, threads per block)
     int block;
-    int tpp_continuity, tpp_momentum, tpp_reinit;
+    int tpp_continuity, tpp_momentum;
     // list_momentum != 0: continuity (one lane) records the neighbour list and momentum
     // reads it (tpp_momentum lanes per particle)
     int list_momentum;
@@ -59,15 +66,21 @@ inline void launch_dep(void (*kernel)(P...), int grid, int block, cudaStream_t s
     cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
 }
 
-// stage 0: continuity + EOS; 1: momentum + integrate (+ next hash); 2: Shepard re-init
+// stage 0: continuity + EOS; 1: momentum + integrate (+ next hash; + Shepard re-init when
+// L.shepard is set)
 void launch_physics_fp64(int stage, const LaunchCtx& L);
 void launch_physics_fp32(int stage, const LaunchCtx& L);
 void launch_physics_fp32_2d(int stage, const LaunchCtx& L);
 void launch_physics_fp32_3d(int stage, const LaunchCtx& L);
 void launch_physics_fp32_list_2d(int stage, const LaunchCtx& L);
 void launch_physics_fp32_list_3d(int stage, const LaunchCtx& L);
+// the momentum gathers of re-initialisation steps (L.shepard set)
+void launch_momentum_fp32_2d_shep(const LaunchCtx& L);
+void launch_momentum_fp32_3d_shep(const LaunchCtx& L);
+void launch_momentum_fp32_list_2d_shep(const LaunchCtx& L);
+void launch_momentum_fp32_list_3d_shep(const LaunchCtx& L);
 
-// Buffer particles after the gathers of a step (K4-K6): move them, copy inlet particles
+// Buffer particles after the gathers of a step (K4-K5): move them, copy inlet particles
 // that crossed into the fluid, move the fluid particles K5 marked to the outlet, drop
 // outlet particles, and sort the buffers by (cell, order) into L.bf2.
 void launch_buffers(const LaunchCtx& L);
@@ -101,6 +114,13 @@ void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out);
 void launch_count_pairs(const LaunchCtx& L, unsigned long long* d_counts);
 
 int scan_max_cells();
+
+// Diagnostics of the cell list (sph_diag.cu) over the sorted particles [b, e) of one
+// scene: the scene-local cell key of each; the number of fluid neighbours each one's
+// gathers accept (counts != null) or their ids written from ids[rows[i - b]] on.
+void launch_cell_keys(const LaunchCtx& L, int32_t b, int32_t e, int32_t* keys);
+void launch_neighbours(const LaunchCtx& L, int32_t b, int32_t e, int32_t* counts, const int64_t* rows,
+                       int32_t* ids);
 
 // Fields interpolated by launch_probe (SPH_PROBE_* codes), at most kMaxProbeFields.
 constexpr int kMaxProbeFields = 8;

@@ -14,6 +14,8 @@
 // rejected with SPH_ERR_ARG.  Every call uses the same array and leaves its contents
 // behind (only the counters are cleared at the start of a call), so calls whose work
 // overlaps on the GPU race with each other: serialise them on one stream.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -189,6 +191,34 @@ void enqueue(const SceneDev& S, const Scratch& s, int32_t n, const double* x, in
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // unique id of the context the address belongs to
+
+// Unique id (for the life of the process) of the calling thread's current CUDA context,
+// through the driver's cuCtxGetCurrent / cuCtxGetId reached by the runtime's entry-point
+// query (no link against the driver library); false when there is none or the query fails.
+bool current_context_id(unsigned long long* id) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)f;
+        cudaGetLastError();
+        resolved = true;
+    }
+    CUcontext ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
 
 int32_t reject(int32_t code, const std::string& msg) {
     set_global_error(msg);
@@ -218,15 +248,21 @@ extern "C" int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, c
     if (dev < 0 || dev >= kMaxDevices) return reject(SPH_ERR_ARG, "sph_count_pairs_noalloc: device index too large");
     unsigned char* base;
     {
-        // set-up, once per device, with that device current: the device address of the
-        // scratch array (its name in host code is not a device address)
+        // set-up, once per device and context, with that device current: the device
+        // address of the scratch array (its name in host code is not a device address).
+        // The address is cached with the id of the context it was taken in; a call from
+        // another context (after cudaDeviceReset, or under a context a caller made current
+        // through the driver API) looks it up again.
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev]) {
+        unsigned long long ctx = 0;
+        const bool known = current_context_id(&ctx);
+        if (!g_scratch_addr[dev] || !known || g_scratch_ctx[dev] != ctx) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess)
                 return reject(SPH_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             g_scratch_addr[dev] = (unsigned char*)p;
+            g_scratch_ctx[dev] = current_context_id(&ctx) ? ctx : 0;
         }
         base = g_scratch_addr[dev];
     }

@@ -234,10 +234,7 @@ __device__ __forceinline__ void carry_frozen(int i, const SceneDev& S, const Sor
     ((V*)nx.v)[i] = ((const V*)st.v)[i];
     nx.rho[i] = st.rho[i];
     if (nx.T) nx.T[i] = st.T[i];
-    const int32_t key = cell_key<DIM>(x, S);
-    sc.key[i] = key;
-    sc.slot[i] = atomicAdd(sc.count + key, 1);
-    count_tile(sc.tile_acc, key);
+    cell_arrival(sc, i, cell_key<DIM>(x, S));
 }
 
 // ---------------------------------------------------------------- buffer neighbours

@@ -38,9 +38,7 @@ __global__ void k_hash(const SceneDev* __restrict__ scenes, NextState nx, Sorted
         return;
     }
     const V x = ((const V*)nx.x)[i];
-    const int32_t key = cell_key<DIM>(x, S);
-    sc.key[i] = key;
-    sc.slot[i] = atomicAdd(sc.count + key, 1);
+    cell_arrival(sc, i, cell_key<DIM>(x, S));
 }
 
 // ---------------------------------------------------------------- scan

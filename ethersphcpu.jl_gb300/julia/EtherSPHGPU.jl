@@ -12,7 +12,9 @@
   The `check::Function` keyword cannot run on the device; pass `aabb = (lo, hi)` (a
   particle is deleted at a check step when a coordinate is > hi or < lo), which is what
   the examples' check functions express (CollapseDry.jl:119-127).  A `check` function
-  given without `aabb` is applied on the host at output steps only.
+  given without `aabb` runs on the host at every check step, as the reference runs it
+  (FluidWallSolve.jl:73-81): the steps run in chunks that end at check steps, the live
+  fluid is downloaded, the closure deletes, and the survivors are uploaded again.
 
   With `staged_output = true` (the default when no host-side check is needed) the files
   are written by the library (sph_output_*): the state after an output step is copied on
@@ -119,12 +121,13 @@ function checkStatus(h, rc)
     return nothing
 end
 
-stack(ps, f) = reduce(hcat, [collect(Float64, getfield(p, f)) for p in ps])  # dim x n
+# dim x n (an empty group gives a 0 x 0 matrix: the library reads no element of it)
+stack(ps, f) = isempty(ps) ? zeros(0, 0) : reduce(hcat, [collect(Float64, getfield(p, f)) for p in ps])
 
 function uploadFluid(h, fluid)
     x, v = stack(fluid, :x_vec_), stack(fluid, :v_vec_)
     sc(f) = Float64[getfield(p, f) for p in fluid]
-    th = fluid[1] isa ThermalLiquidParticle
+    th = eltype(fluid) <: ThermalLiquidParticle
     t, kappa, cp = th ? (sc(:t_), sc(:kappa_), sc(:cp_)) : (C_NULL, C_NULL, C_NULL)
     checkStatus(h, ccall((:sph_upload_fluid, libsph), Int32,
         (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
@@ -147,11 +150,12 @@ end
 
 # Copy the live particles back into the Julia vector (deleteat! for removed ones).
 function downloadFluid!(h, fluid)
+    isempty(fluid) && return nothing  # nothing left to update (every particle was deleted)
     cap = length(fluid)
     dim = length(fluid[1].x_vec_)
     x, v = zeros(dim, cap), zeros(dim, cap)
     rho, p, c, m, gap = zeros(cap), zeros(cap), zeros(cap), zeros(cap), zeros(cap)
-    th = fluid[1] isa ThermalLiquidParticle
+    th = eltype(fluid) <: ThermalLiquidParticle
     t = th ? zeros(cap) : C_NULL
     n = Ref{Int64}(0)
     checkStatus(h, ccall((:sph_download_fluid, libsph), Int32,
@@ -199,7 +203,8 @@ function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, ch
     nw = sum(length, wall_groups; init = 0)
     checkStatus(C_NULL, ccall((:sph_create, libsph), Int32, (Ref{SphParams}, Int64, Int64, Ref{Ptr{Cvoid}}),
         prm, length(fluid), nw, h))
-    staged = staged_output && (aabb !== nothing || check === defaultCheck)
+    host_check = aabb === nothing && check !== defaultCheck  # a closure: run on the host at check steps
+    staged = staged_output && !host_check
     try
         foreach(g -> uploadWalls(h[], g), wall_groups)
         uploadFluid(h[], fluid)
@@ -214,24 +219,38 @@ function runSolve!(solve_code, fluid, wall_groups, kernel, model, td, vtp_io, ch
             assureDirPathExist(vtp_io)
             writeVTP(0, 0.0, vtp_io, [[fluid]; wall_groups])
         end
+        nextStop(step, interval) = (div(step - 1, interval) + 1) * interval
         step = 1
         while step <= td.total_step_
-            last = min(td.total_step_, (div(step - 1, td.output_interval_) + 1) * td.output_interval_)
+            # chunks end at output steps, and at check steps when the closure runs here
+            last = min(td.total_step_, nextStop(step, td.output_interval_))
+            host_check && (last = min(last, nextStop(step, td.check_interval_)))
+            fresh = false  # `fluid` holds the device state
             try
                 checkStatus(h[], ccall((:sph_step, libsph), Int32, (Ptr{Cvoid}, Int64, Int64), h[], step, last - step + 1))
-            catch e  # FluidWallSolve.jl:130-134: report and continue
+            catch e  # FluidWallSolve.jl:130-133: report, write the state of the failing step, continue
                 println(e)
                 println("Error at step: ", last)
+                if staged
+                    outputWrite(h[], last, last * td.dt_)
+                else
+                    downloadFluid!(h[], fluid)
+                    fresh = true
+                    writeVTP(last, last * td.dt_, vtp_io, [[fluid]; wall_groups])
+                end
+            end
+            if host_check && isCheckStep(last, td)  # deleteat!(fluid, !check) (FluidWallSolve.jl:73-81)
+                fresh || downloadFluid!(h[], fluid)
+                n_before = length(fluid)
+                deleteat!(fluid, findall(p -> !check(p), fluid))
+                length(fluid) != n_before && uploadFluid(h[], fluid)
+                fresh = true
             end
             if isOutputStep(last, td)
                 if staged  # the library copies the state and writes while the next steps run
                     outputWrite(h[], div(last, td.output_interval_), last * td.dt_)
                 else
-                    downloadFluid!(h[], fluid)
-                    if aabb === nothing && check !== defaultCheck
-                        deleteat!(fluid, findall(p -> !check(p), fluid))
-                        uploadFluid(h[], fluid)
-                    end
+                    fresh || downloadFluid!(h[], fluid)
                     writeVTP(div(last, td.output_interval_), last * td.dt_, vtp_io, [[fluid]; wall_groups])
                 end
             end

@@ -23,7 +23,7 @@ import numpy as np
 
 from . import _abi
 from .types import (AABBCheck, CompulsiveWallParticles, StaticVelocityWallParticles, ThermostaticWallParticles,
-                    isOutputStep)
+                    isCheckStep, isOutputStep)
 
 
 def make_params(kernel, model, td, *, solve: int, precision: int = _abi.PRECISION_FP64, check: AABBCheck | None = None,
@@ -237,6 +237,31 @@ class Simulation:
         self._check(self.lib.sph_count_pairs(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def cell_keys(self) -> tuple[np.ndarray, tuple]:
+        """Cell of every live fluid particle as the step's sort assigns it (scene-local
+        index cx + nx (cy + ny cz)), rows in download order; and the grid (nx, ny, nz)."""
+        n = C.c_int64()
+        grid = (C.c_int32 * 3)()
+        self._check(self.lib.sph_download_cell_keys(self.h, 0, C.byref(n), None, grid))
+        keys = np.zeros(n.value, dtype=np.int64)
+        self._check(self.lib.sph_download_cell_keys(self.h, n.value, C.byref(n),
+                                                    keys.ctypes.data_as(C.POINTER(C.c_int64)), grid))
+        return keys, tuple(grid)
+
+    def neighbour_lists(self) -> tuple[np.ndarray, np.ndarray]:
+        """Fluid neighbours each live particle's gathers accept, as (offsets[n+1], ids):
+        the ids of row q are those of particle q of download(), ascending."""
+        P64 = C.POINTER(C.c_int64)
+        n, total = C.c_int64(), C.c_int64()
+        cap = int(self.stats().n_fluid) + 1
+        offsets = np.zeros(cap, dtype=np.int64)
+        self._check(self.lib.sph_download_neighbours(self.h, cap, 0, C.byref(n), C.byref(total),
+                                                     offsets.ctypes.data_as(P64), None))
+        ids = np.zeros(max(total.value, 1), dtype=np.int64)
+        self._check(self.lib.sph_download_neighbours(self.h, cap, total.value, C.byref(n), C.byref(total),
+                                                     offsets.ctypes.data_as(P64), ids.ctypes.data_as(P64)))
+        return offsets[:n.value + 1], ids[:total.value]
+
     def stream(self) -> int:
         s = C.c_void_p()
         self._check(self.lib.sph_get_stream(self.h, C.byref(s)))
@@ -289,10 +314,55 @@ def _variant(walls):
     return _abi.SOLVE_FLUID_WALL
 
 
-def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: int = _abi.PRECISION_FP64,
+class ParticleView:
+    """One fluid particle of a downloaded state, with the field names of the reference's
+    particle structs (x_vec_, v_vec_, rho_, p_, c_, mass_, gap_, and t_, kappa_, cp_ for
+    thermal particles): what a `check(p)` closure of solve! reads (CollapseDry.jl:119-127)."""
+
+    __slots__ = ("_d", "_q")
+    _names = {"x_vec_": "x", "v_vec_": "v", "rho_": "rho", "p_": "p", "c_": "c", "mass_": "mass", "gap_": "gap",
+              "t_": "t", "kappa_": "kappa", "cp_": "cp"}
+
+    def __init__(self, d: dict, q: int):
+        self._d = d
+        self._q = q
+
+    def __getattr__(self, name):
+        try:
+            return self._d[ParticleView._names[name]][self._q]
+        except KeyError:
+            raise AttributeError(name) from None
+
+
+def _host_check(sim, check, fluid_type, dim) -> int:
+    """Apply a `check(p) -> Bool` closure on the host at a check step (FluidWallSolve.jl:
+    73-81: every fluid particle with !check(p) is deleted): download the live fluid, keep
+    the particles the closure accepts and, when some fail, upload the survivors in their
+    order (their ids stay ascending, so the sort order and the continuation of the run are
+    unchanged).  Returns the number of particles deleted."""
+    d = sim.download()
+    n = len(d["rho"])
+    keep = np.fromiter((bool(check(ParticleView(d, q))) for q in range(n)), dtype=bool, count=n)
+    dropped = int(n - np.count_nonzero(keep))
+    if dropped:
+        sub = fluid_type(int(np.count_nonzero(keep)), dim)
+        for f, k in ParticleView._names.items():
+            if k in d and hasattr(sub, f):
+                getattr(sub, f)[:] = d[k][keep]
+        sim.upload_fluid(sub)
+    return dropped
+
+
+def solve(fluid, *args, check=None, vtp_io=None, precision: int = _abi.PRECISION_FP64,
           domain_lo=None, domain_hi=None, periodic_x: bool = False, first_step: int = 1, nsteps: int | None = None,
           staged_output: bool = True, wall_time: str | None = None, autotune: bool = False):
     """GPU counterpart of solve!(fluid, walls..., kernel, model, td, vtp_io; check).
+
+    `check`: an AABBCheck (evaluated on the device, in the step's momentum epilogue) or
+    any callable check(p) -> bool over one particle (a ParticleView: p.x_vec_, p.rho_,
+    ...), which runs on the host at every check step (isCheckStep), as the reference runs
+    its closure (FluidWallSolve.jl:73-81): the run stops after each check step, the
+    closure sees the end-of-step state, and the particles it rejects are removed.
 
     Runs steps first_step .. td.total_step_ (or `nsteps` steps), writes VTP files at
     step 0 and at output steps when `vtp_io` is given (FluidWallSolve.jl:95,133-136),
@@ -313,7 +383,9 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
         pad = 2.0 * kernel.influence_radius_
         domain_lo = pts.min(axis=0) - pad if domain_lo is None else domain_lo
         domain_hi = pts.max(axis=0) + pad if domain_hi is None else domain_hi
-    params = make_params(kernel, model, td, solve=variant, precision=precision, check=check,
+    host_check = check if (check is not None and not isinstance(check, AABBCheck)) else None
+    params = make_params(kernel, model, td, solve=variant, precision=precision,
+                         check=None if host_check is not None else check,
                          domain_lo=list(domain_lo), domain_hi=list(domain_hi), periodic_x=periodic_x)
     nw = sum(len(w) for w in walls)
     with Simulation(params, max(len(fluid), 1), nw) as sim:
@@ -331,15 +403,21 @@ def solve(fluid, *args, check: AABBCheck | None = None, vtp_io=None, precision: 
         last = td.total_step_ if nsteps is None else first_step + nsteps - 1
         step = first_step
         while step <= last:
-            # run up to the next output step (isOutputStep, TimeDiscretization.jl:13-18)
+            # run up to the next output step (isOutputStep, TimeDiscretization.jl:13-18) or,
+            # with a host closure, the next check step (isCheckStep, :20-25)
             nxt = step
-            while nxt < last and not (vtp_io is not None and isOutputStep(nxt, td)):
+            while nxt < last and not (vtp_io is not None and isOutputStep(nxt, td)) and \
+                    not (host_check is not None and isCheckStep(nxt, td)):
                 nxt += 1
             if staged:
                 _abi.check(sim.lib, sim.h, sim.lib.sph_step_async(sim.h, step, nxt - step + 1))
             else:
                 sim.step(step, nxt - step + 1)
             step = nxt + 1
+            if host_check is not None and isCheckStep(nxt, td):  # deleteat! before writeVTP
+                if staged:
+                    _abi.check(sim.lib, sim.h, sim.lib.sph_synchronize(sim.h))
+                _host_check(sim, host_check, type(fluid), sim.dim)
             if vtp_io is not None and isOutputStep(nxt, td):
                 if staged:
                     sim.output_write(nxt // td.output_interval_, nxt * td.dt_)

@@ -213,6 +213,31 @@ int32_t sph_stats(SphHandle* h, SphStats* out);
  * pairs within r_cut at the current positions. */
 int32_t sph_count_pairs(SphHandle* h, int64_t* fluid_pairs, int64_t* wall_pairs);
 
+/* Diagnostic: the cell of every live fluid particle at the current positions, as the
+ * step's sort assigns it — the scene-local index cx + nx (cy + ny cz) in the handle's
+ * grid (cells of edge r_cut (1 + 1e-9) / cell_subdivision from domain_lo, positions
+ * outside the grid clamped into its edge cells, a periodic x axis cut into equal cells).
+ * Rows in the order of sph_download_fluid (ascending particle id).  grid (may be NULL)
+ * receives the cell counts (nx, ny, nz).  With keys == NULL only n_out and grid are
+ * written.  Single-scene handles.  Replaces nothing in the
+ * reference's API: it exposes the cell assignment that CellListMap.update! makes inside
+ * each step (FluidWallSolve.jl:21-27) so it can be pinned particle by particle. */
+int32_t sph_download_cell_keys(SphHandle* h, int64_t capacity, int64_t* n_out, int64_t* keys, int32_t* grid);
+
+/* Diagnostic: the fluid neighbours of every live fluid particle that the handle's gathers
+ * accept — every j != i with |x_i - x_j|^2 <= r_cut^2, decided in FP64 (products and sums
+ * rounded one by one, minimum image along a periodic x) for the FP64 form and in FP32 on
+ * cell-relative positions for the FP32-compensated form — as particle ids (those of
+ * sph_download_ids), ascending within a row; rows in the order of sph_download_fluid.
+ * CSR form: offsets[0..n] (capacity: room for n + 1 offsets), ids[offsets[n]].  With
+ * ids == NULL only n_out, offsets and total_out are written; SPH_ERR_ARG when the total
+ * exceeds ids_capacity (total_out is still set).  Single-scene handles.  Replaces nothing
+ * in the reference's API: the per-particle form of the pair list that
+ * CellListMap.neighborlist! + findNeighbours! build each step (FluidWallSolve.jl:28-35,
+ * Neighbour.jl:88-128), for pinning the neighbour search particle by particle. */
+int32_t sph_download_neighbours(SphHandle* h, int64_t capacity, int64_t ids_capacity, int64_t* n_out,
+                                int64_t* total_out, int64_t* offsets, int64_t* ids);
+
 /* The cudaStream_t the handle launches on (for CUDA-event timing by the caller). */
 int32_t sph_get_stream(SphHandle* h, void** stream);
 
@@ -226,7 +251,8 @@ enum {
     SPH_STAGE_SORT = 2,       /* stable (cell, id) placement + reorder      */
     SPH_STAGE_CONTINUITY = 3, /* continuity gather + density + EOS          */
     SPH_STAGE_MOMENTUM = 4,   /* momentum gather + integration              */
-    SPH_STAGE_REINIT = 5      /* Shepard density re-initialisation gather  */
+    SPH_STAGE_REINIT = 5      /* the momentum gather of a density re-initialisation step:
+                                 momentum + integration with the Shepard sums fused in */
 };
 int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out);
 
@@ -292,20 +318,21 @@ int32_t sph_batch_free(SphHandle* h, int64_t* out);
  * The cell list lives in one static device array of the library (about 10 MB, resident
  * on every GPU that loaded the library until the process exits): at most 262,144 fluid
  * and 262,144 wall particles and 262,144 grid cells; larger inputs return SPH_ERR_ARG.
- * The first call on a device looks up that array's device address (make it before any
- * stream capture).  All calls share the array: calls that overlap on the GPU race, so
+ * The first call in a CUDA context looks up that array's device address and caches it
+ * with the context's id (a call from another context, e.g. after cudaDeviceReset, looks
+ * it up again): make the first call before any stream capture.  All calls share the array: calls that overlap on the GPU race, so
  * serialise them on one stream.  Errors: sph_last_error(NULL). */
 int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double* x, int64_t n_wall,
                                 const double* wall_x, int64_t* counts, void* stream);
 
-/* Autotuner of the FP32-compensated form: times the continuity, momentum and Shepard
- * gathers on the current state for every lanes-per-particle count {-1, 1, 2, 4, 8} and
- * block size {64, 128, 256}, and the neighbour-list pair (continuity recording the list
- * with lanes {-1, 1}, momentum reading it with lanes {-1, 1, 2, 4}); keeps the faster of
- * the cell-walk and list pairs, the fastest Shepard shape, and rebuilds the step graphs.
- * out[4] (may be NULL) receives (continuity lanes, momentum lanes, Shepard lanes, block
- * size).  The fluid state is left unchanged.  No-op for the FP64 form, which keeps one
- * thread per particle so that its summation order is fixed. */
+/* Autotuner of the FP32-compensated form: times the continuity and momentum gathers on
+ * the current state for every lanes-per-particle count {-1, 1, 2, 4, 8} and block size
+ * {64, 128, 256}, and the neighbour-list pair (continuity recording the list with lanes
+ * {-1, 1}, momentum reading it with lanes {-1, 1, 2, 4}); keeps the faster of the
+ * cell-walk and list pairs and rebuilds the step graphs.  out[4] (may be NULL) receives
+ * the launch shape (see sph_set_launch_shape).  The fluid state is left unchanged.  No-op
+ * for the FP64 form, which keeps one thread per particle so that its summation order is
+ * fixed. */
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 
 /* Momentum lanes code of the neighbour list: SPH_LANES_LIST + t, t in {1, 2, 4, -1}.
@@ -319,8 +346,9 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 #define SPH_LANES_LIST 16
 
 /* Set the FP32 launch shape by hand (a new handle starts at (1, 1, 1, 128)):
- * shape[4] = (continuity lanes, momentum lanes,
- * Shepard lanes, block size); lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
+ * shape[4] = (continuity lanes, momentum lanes, unused, block size).  shape[2] is kept for
+ * the layout and must be a lanes code: the Shepard sums of a re-initialisation step run
+ * inside the momentum gather, at its lanes.  Lanes in {1, 2, 4, 8} or -1 (one lane whose candidate loop
  * is software-pipelined: loads of the next neighbour overlap the current one's
  * arithmetic; momentum lanes -1 take blocks of at most 256), block in {32, 64, ..., 1024}
  * and a multiple of 32.  Momentum lanes may instead be a neighbour-list code

@@ -56,6 +56,9 @@ def lib() -> C.CDLL:
                                               C.POINTER(C.c_int64)]
         L.or_pair_list_bruteforce.restype = C.c_int64
         L.or_cell_keys.argtypes = [C.c_void_p, C.c_int64, _DP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.or_neighbour_lists.argtypes = [C.c_void_p, C.c_int64, _DP, C.c_int64, C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int64)]
+        L.or_neighbour_lists.restype = C.c_int64
         L.or_neighbour_counts.argtypes = [C.c_void_p, C.c_int64, _DP, C.c_int64, _DP, C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]
         L.or_run_io.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.c_int64] + [_DP] * 7 + \
@@ -119,6 +122,20 @@ def cell_keys(params, x: np.ndarray):
     assert lib().or_cell_keys(C.byref(params), len(x), _p(x), keys.ctypes.data_as(C.POINTER(C.c_int64)),
                               C.byref(nc)) == 0
     return keys, nc.value
+
+
+def neighbour_lists(params, x: np.ndarray):
+    """Full neighbour list of every particle (ids ascending) as (offsets[n+1], ids)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n = len(x)
+    offsets = np.zeros(n + 1, dtype=np.int64)
+    P64 = C.POINTER(C.c_int64)
+    total = lib().or_neighbour_lists(C.byref(params), n, _p(x), 0, offsets.ctypes.data_as(P64), None)
+    assert total >= 0
+    ids = np.zeros(max(total, 1), dtype=np.int64)
+    assert lib().or_neighbour_lists(C.byref(params), n, _p(x), total, offsets.ctypes.data_as(P64),
+                                    ids.ctypes.data_as(P64)) == total
+    return offsets, ids[:total]
 
 
 def neighbour_counts(params, x, wx):

@@ -1131,6 +1131,47 @@ int or_cell_keys(const SphParams* prm, int64_t n, const double* x, int64_t* keys
     return 0;
 }
 
+// Full neighbour list of every particle (all j != i with d^2 <= r_cut^2 at the positions
+// x, minimum image along a periodic x axis), ids ascending, in CSR form: offsets[n + 1],
+// ids[offsets[n]].  The per-particle pair-set pin of the neighbour search
+// (CellListMap.neighborlist! + findNeighbours!, Neighbour.jl:88-128, turned into the
+// full list each particle gathers over).  Returns the total, or -1 on a bad parameter
+// block; ids are written only when the total fits cap.
+int64_t or_neighbour_lists(const SphParams* prm, int64_t n, const double* x, int64_t cap, int64_t* offsets,
+                           int64_t* ids) {
+    Model M;
+    Kern K;
+    if (!load_model(prm, &M, &K)) return -1;
+    Grid G = make_grid(M, K.rc);
+    const int dim = M.dim;
+    const double rc2 = K.rc * K.rc;
+    CellList CL = build_cells(G, n, x, dim, nullptr);
+    std::vector<std::vector<int64_t>> rows((size_t)n);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t c[3];
+        cell_of(G, x + i * dim, c);
+        int64_t cells[kMaxCells];
+        const int nc = neighbour_cells(G, c, cells);
+        std::vector<int64_t>& row = rows[(size_t)i];
+        for (int q = 0; q < nc; ++q)
+            for (int64_t s = CL.start[cells[q]]; s < CL.start[cells[q] + 1]; ++s) {
+                const int64_t j = CL.order[s];
+                if (j == i) continue;
+                double rv[3];
+                rvec(G, x + i * dim, x + j * dim, dim, rv);
+                if (dist2(rv, dim) <= rc2) row.push_back(j);
+            }
+        std::sort(row.begin(), row.end());
+    }
+    offsets[0] = 0;
+    for (int64_t i = 0; i < n; ++i) offsets[i + 1] = offsets[i] + (int64_t)rows[(size_t)i].size();
+    const int64_t total = offsets[n];
+    if (ids && total <= cap)
+        for (int64_t i = 0; i < n; ++i) std::copy(rows[(size_t)i].begin(), rows[(size_t)i].end(), ids + offsets[i]);
+    return total;
+}
+
 // Number of fluid neighbours (full list) of every particle and fluid-wall neighbours.
 int or_neighbour_counts(const SphParams* prm, int64_t n, const double* x, int64_t nw, const double* wx,
                         int64_t* ff_pairs, int64_t* fw_pairs) {

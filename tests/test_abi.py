@@ -183,3 +183,50 @@ def test_julia_binding_names_declared_entry_points_and_fields():
         c_body = re.sub(r"/\*.*?\*/", "", c_body, flags=re.S)
         c_fields = re.findall(r"\b(\w+)(?:\[\d\])?\s*;", c_body)
         assert jl_fields == c_fields, name
+
+
+def _c_prototypes():
+    """name -> (return type, [parameter types]) of every entry point of the header."""
+    hdr = (ROOT / "include" / "ethersph_gpu.h").read_text()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    protos = {}
+    for ret, name, params in re.findall(r"([A-Za-z_][\w \*]*?)\s*\b(sph_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        ps = []
+        for prm in params.split(","):
+            prm = " ".join(prm.split())
+            if prm in ("", "void"):
+                continue
+            ps.append(re.sub(r"\s*\b\w+$", "", prm))  # drop the parameter name
+        protos[name] = (" ".join(ret.split()), ps)
+    return protos
+
+
+def _julia_types_for(ctype):
+    c = ctype.replace("const", "").replace(" ", "")
+    base = {"int32_t": {"Int32"}, "int64_t": {"Int64"}, "double": {"Float64"}, "char*": {"Cstring"},
+            "char**": {"Ptr{Cstring}"}, "void*": {"Ptr{Cvoid}"}, "void**": {"Ref{Ptr{Cvoid}}", "Ptr{Ptr{Cvoid}}"},
+            "SphHandle*": {"Ptr{Cvoid}"},
+            "SphHandle**": {"Ref{Ptr{Cvoid}}", "Ptr{Ptr{Cvoid}}"}}
+    if c in base:
+        return base[c]
+    m = re.fullmatch(r"(\w+)\*", c)
+    jl = {"double": "Float64", "int64_t": "Int64", "int32_t": "Int32"}.get(m.group(1), m.group(1)) if m else None
+    assert jl, ctype
+    return {f"Ptr{{{jl}}}", f"Ref{{{jl}}}"}
+
+
+def test_julia_ccall_types_match_the_header_prototypes():
+    # every ccall of the Julia binding passes the argument and return types the header
+    # declares (arity, widths, pointer element types), so the binding cannot drift from
+    # the C ABI unnoticed while no Julia is available to run it
+    jl = (ROOT / "ethersphcpu.jl_gb300" / "julia" / "EtherSPHGPU.jl").read_text()
+    protos = _c_prototypes()
+    calls = re.findall(r"ccall\(\(:(sph_\w+), libsph\),\s*(\w+),\s*\(([^()]*)\)", jl, flags=re.S)
+    assert len(calls) >= 20
+    for name, ret, types in calls:
+        c_ret, c_params = protos[name]
+        jl_types = [" ".join(x.split()) for x in types.split(",") if x.strip()]
+        assert len(jl_types) == len(c_params), (name, jl_types, c_params)
+        assert ret in _julia_types_for(c_ret), (name, ret, c_ret)
+        for k, (a, c) in enumerate(zip(jl_types, c_params)):
+            assert a in _julia_types_for(c), (name, k, a, c)

@@ -160,16 +160,19 @@ def test_serving_loop_runs_a_poisson_stream(pkg):
     assert s["latency_p99_s"] >= s["latency_p50_s"] > 0
     for c in rep.completed:
         assert np.all(np.isfinite(c.result["x"]))
-    # every result equals the same request run alone
-    c = rep.completed[0]
-    scene = c.request.build()
-    alone = serve_alone(pkg, scene, c.request.nsteps)
-    assert equal(alone, c.result)
+    # every result equals the same request run alone (bit for bit: a scene's sums only
+    # see its own particles and constants, whatever else shares the batch)
+    assert len(rep.completed) == len(reqs)
+    for c in rep.completed:
+        scene = c.request.build()
+        alone = serve_alone(pkg, scene, c.request.nsteps)
+        assert equal(alone, c.result), c.request
 
 
 def serve_alone(pkg, scene, nsteps):
     from ethersph_gb300 import batch, serve
-    with batch.Batch(scene.params(precision=1), scene.n_fluid + 10, 500_000, scene.n_wall + 10, 2) as bt:
+    cells = batch.footprint(scene, 1)[1]
+    with batch.Batch(scene.params(precision=1), scene.n_fluid + 10, cells + 16, scene.n_wall + 10, 2) as bt:
         bt.set_launch_shape(*serve.DEFAULT_LAUNCH_SHAPE)  # the server's shape
         sid = bt.add_scene(scene, 1, nsteps)
         steps = 0

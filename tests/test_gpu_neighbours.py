@@ -1,0 +1,144 @@
+"""The neighbour search particle by particle: cell keys and per-particle neighbour sets.
+
+The benchmark spec asks for the cell assignment and the neighbour pair set of every particle
+to be exact against the reference's neighbour search (CellListMap.neighborlist! +
+findNeighbours!, FluidWallSolve.jl:21-35, Neighbour.jl:88-128).  The library's
+diagnostic entry points (sph_download_cell_keys, sph_download_neighbours) return what the
+step's sort and gathers use; the oracle restates the grid (or_cell_keys) and the full
+neighbour list d^2 <= r_cut^2 (or_neighbour_lists) in FP64 on the same positions.
+
+* FP64 form: keys and neighbour sets equal the oracle's exactly, on lattices (pairs at
+  exactly r_cut), jittered sets, particles clamped into the grid's edge cells, periodic
+  rows, both cell subdivisions, 2D and 3D, and after steps of the dynamics.
+* FP32-compensated form: keys exact (they are hashed from the FP64 masters); its pair
+  test runs in FP32 on cell-relative positions, so its sets may differ from the FP64 sets
+  only by pairs whose distance is within 1e-5 r_cut^2 of r_cut^2 (tolerance stated here).
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP32_EDGE_TOL = 1e-5  # |d^2 / r_cut^2 - 1| of the pairs the two forms may decide differently
+
+
+def scenes_mod():
+    from ethersph_gb300 import scenes
+    return scenes
+
+
+def jittered(s, frac=0.3, seed=7):
+    rng = np.random.default_rng(seed)
+    dx = float(np.min(s.fluid.gap_))
+    s.fluid.x_vec_[:] += rng.uniform(-frac * dx, frac * dx, s.fluid.x_vec_.shape)
+    return s
+
+
+def make(name):
+    sc = scenes_mod()
+    if name == "dam_break_lattice":
+        return sc.dam_break_2d(dx=0.02)
+    if name == "dam_break_jitter":
+        return jittered(sc.dam_break_2d(dx=0.03))
+    if name == "cavity":
+        return sc.natural_convection_2d(n=64)
+    if name == "periodic":
+        return sc.poiseuille_periodic_2d(n_across=16)
+    if name == "dam_break_3d":
+        return sc.dam_break_3d(dx=0.04, tank=(0.6, 0.3, 0.4), column=(0.2, 0.2, 0.3))
+    if name == "dam_break_3d_jitter":
+        return jittered(sc.dam_break_3d(dx=0.04, tank=(0.6, 0.3, 0.4), column=(0.2, 0.2, 0.3)))
+    if name == "clamped_2d":  # the grid ends inside the fluid: keys clamped into the top cells
+        s = sc.dam_break_2d(dx=0.03)
+        return dataclasses.replace(s, domain_hi=(s.domain_hi[0], 1.2), check=None)
+    if name == "clamped_3d":
+        s = sc.dam_break_3d(dx=0.05, tank=(0.6, 0.3, 0.4), column=(0.2, 0.2, 0.3))
+        hi = list(s.domain_hi)
+        hi[1] = 0.15
+        return dataclasses.replace(s, domain_hi=tuple(hi), check=None)
+    raise KeyError(name)
+
+
+def gpu_lists(pkg, s, precision, sub, steps):
+    prm = s.params(precision=precision, cell_subdivision=sub)
+    with pkg.Simulation(prm, s.n_fluid, s.n_wall) as sim:
+        for w in s.walls:
+            sim.upload_walls(w)
+        sim.upload_fluid(s.fluid)
+        if steps:
+            sim.step(1, steps)
+        d = sim.download()
+        ids = sim.download_ids()
+        keys, grid = sim.cell_keys()
+        offsets, nbr = sim.neighbour_lists()
+    return prm, d["x"], ids, keys, grid, offsets, nbr
+
+
+def oracle_lists(orc, prm, x, ids):
+    keys, ncells = orc.cell_keys(prm, x)
+    offsets, nbr = orc.neighbour_lists(prm, x)
+    return keys, ncells, offsets, ids[nbr]  # oracle indices -> particle ids (ascending either way)
+
+
+def rows(offsets, nbr):
+    return [nbr[offsets[q]:offsets[q + 1]] for q in range(len(offsets) - 1)]
+
+
+def d2_ratio(x, q, ids_row, ids, rc, period=None):
+    pos = np.searchsorted(ids, ids_row)
+    rv = x[q] - x[pos]
+    if period is not None:
+        rv[:, 0] = np.where(rv[:, 0] > period / 2, rv[:, 0] - period, rv[:, 0])
+        rv[:, 0] = np.where(rv[:, 0] < -period / 2, rv[:, 0] + period, rv[:, 0])
+    return np.sum(rv * rv, axis=1) / (rc * rc)
+
+
+CASES = ["dam_break_lattice", "dam_break_jitter", "cavity", "periodic", "dam_break_3d", "dam_break_3d_jitter",
+         "clamped_2d", "clamped_3d"]
+
+
+@pytest.mark.parametrize("sub", [1, 2])
+@pytest.mark.parametrize("steps", [0, 40])
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_keys_and_neighbour_sets_equal_the_oracle(pkg, orc, name, steps, sub):
+    s = make(name)
+    prm, x, ids, keys, grid, offsets, nbr = gpu_lists(pkg, s, 0, sub, steps)
+    okeys, ncells, ooff, onbr = oracle_lists(orc, prm, x, ids)
+    assert int(np.prod(grid)) == ncells
+    assert np.array_equal(keys, okeys)
+    assert np.array_equal(offsets, ooff), "neighbour counts differ"
+    assert np.array_equal(nbr, onbr), "neighbour ids differ"
+    assert offsets[-1] > 0
+
+
+@pytest.mark.parametrize("name", ["dam_break_lattice", "dam_break_jitter", "periodic", "dam_break_3d_jitter",
+                                  "clamped_2d"])
+def test_fp32_neighbour_sets_differ_only_at_r_cut(pkg, orc, name):
+    s = make(name)
+    prm, x, ids, keys, grid, offsets, nbr = gpu_lists(pkg, s, 1, 0, 40)
+    okeys, _, ooff, onbr = oracle_lists(orc, prm, x, ids)
+    assert np.array_equal(keys, okeys)
+    rc = prm.influence_radius
+    period = (prm.domain_hi[0] - prm.domain_lo[0]) if prm.periodic_x else None
+    n_diff = 0
+    for q, (a, b) in enumerate(zip(rows(offsets, nbr), rows(ooff, onbr))):
+        if np.array_equal(a, b):
+            continue
+        diff = np.setxor1d(a, b)
+        n_diff += len(diff)
+        ratio = d2_ratio(x, q, diff, ids, rc, period)
+        assert np.all(np.abs(ratio - 1.0) <= FP32_EDGE_TOL), (q, diff, ratio)
+    print(name, "neighbour entries decided differently at r_cut:", n_diff, "of", len(onbr))
+    if "jitter" in name:  # off the lattice, pairs within 1e-5 r_cut^2 of r_cut^2 are rare
+        assert n_diff <= 1e-3 * len(onbr)
+
+
+def test_diagnostics_refuse_batches_and_empty_handles(pkg):
+    s = scenes_mod().dam_break_2d(dx=0.05)
+    with pkg.Simulation(s.params(), s.n_fluid, s.n_wall) as sim:
+        with pytest.raises(pkg.SphError):
+            sim.cell_keys()
+        with pytest.raises(pkg.SphError):
+            sim.neighbour_lists()

@@ -241,6 +241,38 @@ def test_solve_entry_point(pkg, orc):
     compare(got, ref, 1e-12, keys=("x", "v", "rho"))
 
 
+def _slanted(p):
+    # a check closure that is not a box (a slanted plane): the wedge right of it leaves
+    return p.x_vec_[0] < 0.99 - 0.02 * p.x_vec_[1]
+
+
+def test_solve_runs_a_check_closure_at_every_check_step(pkg, orc):
+    # check(p) runs on the host at every check step (check_interval 5 < output_interval
+    # 100), as FluidWallSolve.jl:73-81 runs it; the oracle is stepped the same way: to each
+    # check step with the device box off, then the closure deletes with deleteat! order
+    import dataclasses
+    sc = scenes_mod()
+    s = dataclasses.replace(sc.dam_break_2d(dx=0.04, total_step=60), check=None)
+    assert s.td.check_interval_ == 5 and s.td.output_interval_ > s.td.check_interval_
+    fluid, walls = orc.scene_arrays(s)
+    prm = s.params()
+    step, dropped = 1, 0
+    while step <= 60:
+        nxt = min(60, (step // 5 + 1) * 5 if step % 5 else step)
+        fluid = orc.run(prm, fluid, walls, step, nxt - step + 1, mode=orc.GATHER, threads=8)
+        step = nxt + 1
+        if nxt % 5 == 0:
+            keep = fluid["x"][:, 0] < 0.99 - 0.02 * fluid["x"][:, 1]
+            dropped += int(np.count_nonzero(~keep))
+            fluid = {k: np.ascontiguousarray(a[keep]) for k, a in fluid.items()}
+    assert dropped > 0
+    pkg.solve(s.fluid, s.walls[0], s.kernel, s.model, s.td, check=_slanted, domain_lo=s.domain_lo,
+              domain_hi=s.domain_hi)
+    got = dict(x=s.fluid.x_vec_, v=s.fluid.v_vec_, rho=s.fluid.rho_, p=s.fluid.p_)
+    assert len(got["rho"]) == len(fluid["rho"])
+    compare(got, fluid, 1e-12, keys=("x", "v", "rho", "p"))
+
+
 def test_download_ids_name_the_survivors(pkg, orc):
     s = scenes_mod().dam_break_2d(dx=0.04)
     s.check = pkg.AABBCheck(hi=(4.0, 1.0))

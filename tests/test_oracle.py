@@ -220,6 +220,44 @@ def test_periodic_pairs_use_minimum_image(pkg, orc):
     assert ff == cnt
 
 
+@pytest.mark.parametrize("case", ["lattice_2d", "jitter_2d", "jitter_3d", "periodic", "clamped"])
+def test_neighbour_lists_equal_bruteforce(pkg, orc, case):
+    # or_neighbour_lists (the per-particle pin the GPU's sets are compared with) against
+    # an all-pairs restatement with the same rounding: d^2 = sum of products, k ascending
+    from ethersph_gb300 import scenes
+    rng = np.random.default_rng(3)
+    period = None
+    if case == "periodic":
+        s = scenes.poiseuille_periodic_2d(n_across=10)
+        period = s.meta["L"]
+        x = s.fluid.x_vec_
+    elif case == "jitter_3d":
+        s = scenes.dam_break_3d(dx=0.05, tank=(0.8, 0.4, 0.4), column=(0.3, 0.2, 0.4))
+        x = s.fluid.x_vec_ + 0.3 * 0.05 * rng.uniform(-1, 1, s.fluid.x_vec_.shape)
+    else:
+        s = scenes.dam_break_2d(dx=0.05)
+        x = s.fluid.x_vec_ + (0.0 if case == "lattice_2d" else 0.3 * 0.05 * rng.uniform(-1, 1, s.fluid.x_vec_.shape))
+    prm = s.params()
+    if case == "clamped":  # the grid ends inside the fluid: keys clamped into the top cells
+        prm.domain_hi[1] = 0.6
+    x = np.ascontiguousarray(x)
+    offsets, ids = orc.neighbour_lists(prm, x)
+    rc = s.kernel.influence_radius_
+    for i in range(len(x)):
+        rv = x[i] - x
+        if period is not None:
+            rv[:, 0] = np.where(rv[:, 0] > period / 2, rv[:, 0] - period,
+                                np.where(rv[:, 0] < -period / 2, rv[:, 0] + period, rv[:, 0]))
+        d2 = rv[:, 0] * rv[:, 0] + rv[:, 1] * rv[:, 1]
+        if x.shape[1] == 3:
+            d2 = d2 + rv[:, 2] * rv[:, 2]
+        expect = np.flatnonzero(d2 <= rc * rc)
+        expect = expect[expect != i]
+        assert np.array_equal(ids[offsets[i]:offsets[i + 1]], expect), i
+    if case == "lattice_2d":  # interior particles: 28 neighbours within 3 dx (4 at exactly 3 dx)
+        assert np.diff(offsets).max() == 28
+
+
 # ---------------------------------------------------------------- step-level
 def _run_both(orc, scene, steps):
     prm = scene.params()

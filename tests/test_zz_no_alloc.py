@@ -16,20 +16,20 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def handle_counts(pkg, scene):
-    with pkg.Simulation(scene.params(), scene.n_fluid, scene.n_wall) as sim:
+def handle_counts(pkg, scene, sub=0):
+    with pkg.Simulation(scene.params(cell_subdivision=sub), scene.n_fluid, scene.n_wall) as sim:
         for w in scene.walls:
             sim.upload_walls(w)
         sim.upload_fluid(scene.fluid)
         return sim.count_pairs()
 
 
-def noalloc_counts(lib, scene, torch):
+def noalloc_counts(lib, scene, torch, sub=0):
     x = torch.from_numpy(np.ascontiguousarray(scene.fluid.x_vec_)).cuda()
     wx = torch.from_numpy(np.ascontiguousarray(np.concatenate([w.x_vec_ for w in scene.walls]))).cuda()
     out = torch.full((2,), -1, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream()
-    prm = scene.params()
+    prm = scene.params(cell_subdivision=sub)
     rc = lib.sph_count_pairs_noalloc(C.byref(prm), len(x), C.c_void_p(x.data_ptr()), len(wx),
                                      C.c_void_p(wx.data_ptr()), C.c_void_p(out.data_ptr()),
                                      C.c_void_p(stream.cuda_stream))
@@ -52,6 +52,48 @@ def test_noalloc_pair_counts_match_handle(pkg):
     assert noalloc_counts(lib, big, torch) == expect_big
     assert noalloc_counts(lib, small, torch) == expect_small
     assert noalloc_counts(lib, big, torch) == expect_big
+
+
+def test_noalloc_other_grids_match_handle(pkg):
+    # the 3D hash and walk, the periodic x wrap of the pair distance, and one cell per
+    # r_cut (reach 1) instead of the default two, each against a regular handle
+    torch = pytest.importorskip("torch")
+    from ethersph_gb300 import _abi, scenes
+    lib = _abi.load_library()
+    cases = [(scenes.dam_break_3d(dx=0.05, tank=(0.6, 0.3, 0.4), column=(0.2, 0.2, 0.3)), 0),
+             (scenes.poiseuille_periodic_2d(n_across=16), 0),
+             (scenes.dam_break_2d(dx=0.04), 1)]
+    for s, sub in cases:
+        expect = handle_counts(pkg, s, sub)
+        assert expect[0] > 0
+        assert noalloc_counts(lib, s, torch, sub) == expect, s.name
+        assert noalloc_counts(lib, s, torch, sub) == expect, s.name
+
+
+def test_noalloc_call_allocates_no_device_memory(pkg):
+    # after a first call (which looks up the scratch array's address), a call leaves the
+    # device's free memory exactly as it was
+    torch = pytest.importorskip("torch")
+    from ethersph_gb300 import _abi, scenes
+    lib = _abi.load_library()
+    s = scenes.dam_break_2d(dx=0.02)
+    x = torch.from_numpy(np.ascontiguousarray(s.fluid.x_vec_)).cuda()
+    wx = torch.from_numpy(np.ascontiguousarray(s.walls[0].x_vec_)).cuda()
+    out = torch.zeros(2, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    prm = s.params()
+
+    def call():
+        rc = lib.sph_count_pairs_noalloc(C.byref(prm), len(x), C.c_void_p(x.data_ptr()), len(wx),
+                                         C.c_void_p(wx.data_ptr()), C.c_void_p(out.data_ptr()),
+                                         C.c_void_p(stream.cuda_stream))
+        assert rc == 0, lib.sph_last_error(None)
+        stream.synchronize()
+
+    call()
+    free_before = torch.cuda.mem_get_info()[0]
+    call()
+    assert torch.cuda.mem_get_info()[0] == free_before
 
 
 def test_noalloc_rejects_sizes_beyond_the_limit(pkg):
