@@ -9,12 +9,19 @@ Compiles every translation unit of ``csrc/`` with nvcc in parallel and links
 """
 from __future__ import annotations
 
-import concurrent.futures as cf
 import os
-import shutil
-import subprocess
 import sys
-from pathlib import Path
+
+# Run as a script, this file's directory would come first on sys.path, and the package's
+# types.py (the mirror of the reference's type tree) would shadow the standard library's
+# `types` module for every import below: drop it.
+if sys.path and os.path.abspath(sys.path[0] or ".") == os.path.dirname(os.path.abspath(__file__)):
+    sys.path.pop(0)
+
+import concurrent.futures as cf  # noqa: E402
+import shutil  # noqa: E402
+import subprocess  # noqa: E402
+from pathlib import Path  # noqa: E402
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"

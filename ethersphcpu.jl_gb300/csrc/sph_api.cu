@@ -198,16 +198,6 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
     S.inv_cp_f = (float)S.inv_cp_d;
     S.inv_rho0 = 1.0 / p.rho_0;
     S.inv_rho0_f = (float)(1.0 / p.rho_0);
-    S.b_f = (float)p.b;
-    S.p0_f = (float)p.p_0;
-    S.eos_poly = p.gamma >= 1 && p.gamma <= 8;
-    if (S.eos_poly) {  // C(gamma, k) = C(gamma, k - 1) (gamma - k + 1) / k, exact in FP32 here
-        double c = 1.0;
-        for (int k = 1; k <= p.gamma; ++k) {
-            c = c * (double)(p.gamma - k + 1) / (double)k;
-            S.eos_c[k - 1] = (float)c;
-        }
-    }
     return true;
 }
 
@@ -1662,11 +1652,9 @@ int32_t sph_time_stages(SphHandle* h, int32_t reps, double* ms_out) {
             case SPH_STAGE_CONTINUITY: launch_physics(0, L); break;
             case SPH_STAGE_MOMENTUM: launch_physics(1, L); break;
             case SPH_STAGE_REINIT: launch_physics(1, Lr); break;
-            case SPH_NUM_STAGES: launch_physics(0, Lr); break;  // continuity forming the Shepard volumes
         }
     };
     for (int stage = 0; stage < SPH_NUM_STAGES; ++stage) {
-        if (stage == SPH_STAGE_REINIT) run(SPH_NUM_STAGES);
         run(stage);  // warm-up
         SPH_CUDA(h, cudaEventRecord(e0, st));
         for (int r = 0; r < reps; ++r) run(stage);

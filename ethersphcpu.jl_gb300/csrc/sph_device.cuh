@@ -87,9 +87,7 @@ struct SceneDev {
     float kw_a_f, kg_a_f, inv_h_f, c0_f, rho0_f, inv_cp_f, inv_rho0_f;
     float rc2_prune;    // rc2_f * (1 + 1e-5): conservative bound for the stencil pruning
     float inv_cell_fx;  // 1 / cell_f[0]
-    float b_f, p0_f;
-    float eos_c[8];     // binomial coefficients C(gamma, k), k = 1..gamma (gamma <= 8)
-    int32_t eos_poly;   // 1: the FP32 equation of state runs on the binomial sum (1 <= gamma <= 8)
+    float pad_f;
 };
 
 // ---------------------------------------------------------------- vector types

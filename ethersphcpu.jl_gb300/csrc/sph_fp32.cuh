@@ -413,12 +413,22 @@ __device__ __forceinline__ void walk_list(const SceneDev& S, const NbrList& nl, 
             d = dn;
         }
     } else {
-        for (int k = lane; k < cnt; k += TPP) {
-            const int32_t x = entry(k);
+        // the next entry is loaded while the current neighbour is processed, so only the
+        // neighbour's own load stays on each iteration's chain of memory round trips
+        int k = lane;
+        if (k >= cnt) return;
+        int32_t x = entry(k);
+        for (;;) {
+            const int kn = k + TPP;
+            const bool more = kn < cnt;
+            const int32_t xn = more ? entry(kn) : 0;
             const int j = i + (x >> 9);
             float ox, oy, oz;
             off(x, ox, oy, oz);
             body(j, load(j), ox, oy, oz, 0);
+            if (!more) break;
+            k = kn;
+            x = xn;
         }
     }
 }
@@ -451,7 +461,7 @@ __device__ __forceinline__ void decode_cell(int32_t key, const SceneDev& S, int3
 // LIST (one lane per particle): also records the neighbours within r_cut in nl.
 template <int DIM, int KK, int TPP, bool PF, bool LIST>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
-                                 BufferState bf, NbrList nl, int force_reinit) {
+                                 BufferState bf, NbrList nl) {
     pdl_wait();
     static_assert(!LIST || TPP == 1, "the neighbour list is written by one lane per particle");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -532,117 +542,34 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         using V = typename VecT<DIM>::T;
         dr += buffer_drho<DIM, KK>(S, bf, c, ((const V*)st.x)[i], ((const V*)st.v)[i]);
     }
-    // updateDensity! (UpdateDensity.jl:8-12) on the FP64 master density, then the Tait
-    // equation of state (UpdatePressure.jl:8-16) in FP32: its p, c and P feed FP32 pair
-    // terms, and FP64 work is slow on GB300.  It is evaluated on the relative change
-    // d = rho/rho0 - 1 (formed in FP64, then rounded), (1 + d)^gamma - 1 as the binomial
-    // sum of C(gamma, k) d^k by Horner, so no FP32 cancellation of (rho/rho0)^gamma - 1
-    // occurs; for gamma above 8 it runs in FP64.  The FP64 Shepard volume m/rho is formed
-    // only on the scene's re-initialisation steps (every step with force_reinit).
+    // Tait equation of state (UpdatePressure.jl:8-16) with one FP64 division and plain
+    // powers: FP64 is slow on GB300, and these values feed FP32 pair terms (P, c) or FP64
+    // sums (vol) where their last-bit differences from the reference's rounding do not show.
+    // (Evaluated in FP32 instead, on the relative change rho/rho0 - 1, it took 4 more
+    // registers and fewer resident warps: slower on GB300.)
     // loads first: stores to the state arrays would otherwise order them (possible aliasing)
     double rho = st.rho[i];
+    const double m_i = st.m[i];
     const float4 fb_i = st.fb[i];
     const float4 fc_i = DIM == 3 ? st.fc[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     rho += dr * S.dt;
-    float p_f, c_f;
-    if (S.eos_poly) {
-        const float d = (float)((rho - S.rho0) * S.inv_rho0);
-        const int g = S.gamma;
-        float acc = S.eos_c[g - 1];
-        for (int k = g - 1; k >= 1; --k) acc = fmaf(acc, d, S.eos_c[k - 1]);
-        p_f = fmaf(S.b_f, acc * d, S.p0_f);
-        const float r1 = 1.f + d;
-        float rp = 1.f;  // (rho/rho0)^((gamma-1) div 2)
-        for (int k = 0; k < (g - 1) >> 1; ++k) rp *= r1;
-        c_f = S.c0_f * ((g & 1) ? rp : sqrtf(rp * rp * r1));
-    } else {
-        const double rr = rho * S.inv_rho0;
-        p_f = (float)(S.b * (powi_plain(rr, S.gamma) - 1.0) + S.p0);
-        c_f = (float)(S.c0 * ((S.gamma & 1) ? powi_plain(rr, (S.gamma - 1) >> 1) : sqrt(powi_plain(rr, S.gamma - 1))));
-    }
-    const float rho_f = (float)rho;
-    const float inv_rho_f = __frcp_rn(rho_f);
-    const float P = p_f * inv_rho_f * inv_rho_f;
+    const double inv_rho = 1.0 / rho;
+    const double rr = rho * S.inv_rho0;
+    const double p = S.b * (powi_plain(rr, S.gamma) - 1.0) + S.p0;
+    const double cs =
+        S.c0 * ((S.gamma & 1) ? powi_plain(rr, (S.gamma - 1) >> 1) : sqrt(powi_plain(rr, S.gamma - 1)));
+    const double P = p * inv_rho * inv_rho;
     st.rhoc[i] = rho;
-    st.p[i] = (double)p_f;
-    st.c[i] = (double)c_f;
-    st.P[i] = (double)P;
-    if (force_reinit || is_step(sc.scene_step[s], S.reinit_interval)) st.vol[i] = st.m[i] / rho;
+    st.p[i] = p;
+    st.c[i] = cs;
+    st.P[i] = P;
+    st.vol[i] = m_i * inv_rho;
     if (DIM == 2) {
-        st.fb[i] = make_float4(fb_i.x, rho_f, P, fb_i.w);
+        st.fb[i] = make_float4(fb_i.x, (float)rho, (float)P, fb_i.w);
     } else {
-        st.fb[i] = make_float4(fb_i.x, fb_i.y, fb_i.z, rho_f);
-        st.fc[i] = make_float4(P, fc_i.y, fc_i.z, fc_i.w);
+        st.fb[i] = make_float4(fb_i.x, fb_i.y, fb_i.z, (float)rho);
+        st.fc[i] = make_float4((float)P, fc_i.y, fc_i.z, fc_i.w);
     }
-}
-
-// -------------------------------------------------------------------- K5 epilogue, split
-// The forward-Euler update of K5 (UpdateTemperature/Velocity/Position.jl) with TPP >= DIM
-// lanes per particle, each lane holding the combined sums: lane k < DIM updates component
-// k of v and x on the FP64 masters, checks it (finite, inside the check box) and takes
-// its cell coordinate; lane 0 gathers those through the group and writes the scalars (T,
-// the density or its Shepard re-initialisation) and the arrival in the next cell list.
-// The same operations as the one-lane epilogue, spread over the components.
-template <int DIM, int MODE, int TPP, bool SHEP>
-__device__ __forceinline__ void momentum_epilogue_split(int i, int lane, const SceneDev& S, const SortedState& st,
-                                                        const NextState& nx, const SortScratch& sc,
-                                                        const Kahan (&dv)[3], const Kahan& dT, double sw, double sws) {
-    constexpr int VS = DIM == 2 ? 2 : 4;  // doubles per stored vector (double2 / double4)
-    const int k = lane;
-    if (k >= DIM) {
-        if (DIM == 3 && k == 3) {  // the unused w of the 3D vectors, as the one-lane epilogue writes it
-            ((double*)nx.x)[(int64_t)i * VS + 3] = 0.0;
-            ((double*)nx.v)[(int64_t)i * VS + 3] = 0.0;
-        }
-        return;
-    }
-    const int base = (int)(threadIdx.x & 31u) & ~(TPP - 1);
-    const unsigned cmask = ((1u << DIM) - 1u) << base;
-    const int64_t step = sc.scene_step[st.scene[i]];
-    // loads first: the stores below would otherwise order them (possible aliasing)
-    const double x0 = ((const double*)st.x)[(int64_t)i * VS + k];
-    const double v0 = ((const double*)st.v)[(int64_t)i * VS + k];
-    const double rho_d = st.rhoc[i];
-    const double T0 = MODE == kModeThermal ? st.T[i] : 0.0;
-    const double dvd = (k == 0 ? dv[0] : (k == 1 ? dv[1] : dv[DIM - 1])).value();
-    const double dt = S.dt;
-    double Tn = 0.0, body;
-    if (MODE == kModeThermal) {  // every component lane forms the same temperature
-        Tn = T0 + dt * dT.value();
-        body = S.bous[k] * (Tn - S.t0);
-    } else {
-        body = S.g[k];
-    }
-    double vn = v0, xn = x0;
-    vn += body * dt;
-    vn += dvd * dt;
-    xn += vn * dt - dvd * S.half_dtdt;  // dv dt^2 / 2
-    if (k == 0 && S.periodic_x) {
-        if (xn >= S.wrap_hi) xn -= S.period;
-        else if (xn < S.lo[0]) xn += S.period;
-    }
-    ((double*)nx.x)[(int64_t)i * VS + k] = xn;
-    ((double*)nx.v)[(int64_t)i * VS + k] = vn;
-    const bool bad = !(bits_finite(xn) & bits_finite(vn));
-    const bool out = S.check_enabled && is_step(step, S.check_interval) && ((xn > S.check_hi[k]) | (xn < S.check_lo[k]));
-    const int32_t ck = cell_coord(xn, S, k);
-    const unsigned bad_lanes = __ballot_sync(cmask, bad) & cmask;
-    const unsigned out_lanes = __ballot_sync(cmask, out) & cmask;
-    const int32_t cy = __shfl_sync(cmask, ck, base + 1);
-    const int32_t cz = DIM == 3 ? __shfl_sync(cmask, ck, base + DIM - 1) : 0;
-    if (k != 0) return;
-    if (MODE == kModeThermal) nx.T[i] = Tn;
-    else if (nx.T) nx.T[i] = st.T[i];
-    double rho_out = rho_d;
-    if constexpr (SHEP) {  // the particle's own W(0) term (ReconstructValue.jl:51-55), then the quotient
-        sw += S.k0 * st.vol[i];
-        sws += S.k0 * st.m[i];
-        rho_out = sws / sw;
-    }
-    nx.rho[i] = rho_out;
-    if ((bad_lanes || !bits_finite(rho_d)) && S.nan_check) atomicOr(sc.status, kStatusNonFinite);
-    if (out_lanes) sc.key[i] = kDeadKey;
-    else cell_arrival(sc, i, S.cell_off + (cz * S.n[1] + cy) * S.n[0] + ck);
 }
 
 // -------------------------------------------------------------------- K5 (FP32)
@@ -888,14 +815,6 @@ __global__ void __launch_bounds__(PF ? 256 : 1024) k_momentum_f32(const SceneDev
         sw = group_sum<TPP>(sw, mask);
         sws = group_sum<TPP>(sws, mask);
     }
-    if constexpr (TPP >= DIM && MODE != kModeBuffers) {
-        // Every lane of the group holds the combined sums: lane k integrates component k in
-        // FP64 and hashes its cell coordinate, so the FP64 work of a particle (GB300's
-        // FP64 pipe is narrow) is spread over DIM lanes instead of left to lane 0 of a
-        // half-idle warp; lane 0 then adds the scalars and the cell arrival.
-        momentum_epilogue_split<DIM, MODE, TPP, SHEP>(i, lane, S, st, nx, sc, dv, dT, sw, sws);
-        return;
-    }
     if (lane != 0) return;
     double dvd[DIM];
 #pragma unroll
@@ -993,7 +912,7 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     if (stage == 0) {
         if constexpr (!SHEP && (!LIST || TPP == 1))
             launch_dep(k_continuity_f32<DIM, KK, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.sc, L.cap,
-                       L.bf, L.nl, L.force_reinit);
+                       L.bf, L.nl);
     } else if (mode == kModeFluidWall) {
         launch_momentum<DIM, KK, kModeFluidWall, TPP, PF, LIST, SHEP>(L, grid, block);
     } else if (mode == kModeWallPressure) {
