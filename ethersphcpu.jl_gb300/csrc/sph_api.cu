@@ -1741,8 +1741,8 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out) {
         const Best m_walk = search(1, walk_tpps, 5, false);
         Best c_list, m_list;
         if (have_list) {
-            const int c_tpps[2] = {-1, 1}, m_tpps[4] = {-1, 1, 2, 4};
-            c_list = search(0, c_tpps, 2, true);
+            const int c_tpps[3] = {-1, 1, 2}, m_tpps[4] = {-1, 1, 2, 4};
+            c_list = search(0, c_tpps, 3, true);
             // the momentum trials read the list the last continuity trial recorded
             trial(0, c_list.tpp, c_list.block, true);
             m_list = search(1, m_tpps, 4, true);
@@ -1817,8 +1817,8 @@ int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape) {
         const int t = shape[1] - SPH_LANES_LIST;
         if (t != -1 && t != 1 && t != 2 && t != 4)
             return fail(h, SPH_ERR_ARG, "neighbour-list momentum lanes must be SPH_LANES_LIST + 1, 2, 4 or -1");
-        if (shape[0] != 1 && shape[0] != -1)
-            return fail(h, SPH_ERR_ARG, "the neighbour list is recorded by one continuity lane (1 or -1)");
+        if (shape[0] != 1 && shape[0] != -1 && shape[0] != 2)
+            return fail(h, SPH_ERR_ARG, "the neighbour list is recorded by one or two continuity lanes (1, -1 or 2)");
     } else if (!walk_code(shape[1])) {
         return fail(h, SPH_ERR_ARG, "lanes per particle must be 1, 2, 4, 8 or -1 (one pipelined lane)");
     }

@@ -157,8 +157,11 @@ struct WallState {
 // change between the two gathers).  Entry k of particle i is e[k * stride + i] =
 // (j - i) << 9 | (dz + m) << 6 | (dy + m) << 3 | (dx + m): j the sorted index of the
 // neighbour, (dx, dy, dz) the offset of j's cell from i's cell, m the reach in cells.
-// n[i] = the number of entries, or kListWalk when they do not fit (more than kmax
-// neighbours, j - i outside 23 bits, or m > 3): momentum then walks the cells for i.
+// A one-lane writer fills entries 0, 1, ...; with two lanes, lane 0 fills them from 0 up
+// and lane 1 from kmax - 1 down.  n[i] = front | back << 16 (the entries written by the
+// two lanes), or kListWalk when they do not fit (more than kmax neighbours, j - i outside
+// 23 bits, or m > 3): momentum then walks the cells for i.  The list of i reads as
+// entries 0 .. front - 1, then kmax - 1 down to kmax - back.
 struct NbrList {
     int32_t* e;
     int32_t* n;

@@ -380,7 +380,10 @@ template <int DIM, int TPP, bool PF, typename L, typename F>
 __device__ __forceinline__ void walk_list(const SceneDev& S, const NbrList& nl, int i, int cnt, int lane, L&& load,
                                           F&& body) {
     const int m = S.reach;
-    auto entry = [&](int k) { return __ldg(list_entry(nl, k, i)); };
+    // the list is entries [0, front) followed by entries kmax - 1 down to kmax - back
+    const int front = cnt & 0xffff, back = cnt >> 16;
+    cnt = front + back;
+    auto entry = [&](int k) { return __ldg(list_entry(nl, k < front ? k : nl.kmax - 1 - (k - front), i)); };
     auto off = [&](int32_t x, float& ox, float& oy, float& oz) {
         ox = cell_offset((x & 7) - m, S.cell_f[0]);
         oy = cell_offset(((x >> 3) & 7) - m, S.cell_f[1]);
@@ -463,7 +466,7 @@ template <int DIM, int KK, int TPP, bool PF, bool LIST>
 __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedState st, SortScratch sc, int32_t cap,
                                  BufferState bf, NbrList nl) {
     pdl_wait();
-    static_assert(!LIST || TPP == 1, "the neighbour list is written by one lane per particle");
+    static_assert(!LIST || TPP <= 2, "the neighbour list is written by one or two lanes per particle");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = t / TPP, lane = t % TPP;
     if (i >= cap || i >= *sc.n_live) return;
@@ -486,7 +489,10 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
     Kahan drho;
     int cnt = 0;
     bool list_ok = !LIST || S.reach <= 3;
-    int32_t* lp = LIST ? nl.e + i : nullptr;
+    // lane 0 fills the particle's list from entry 0 up, lane 1 (two-lane writer) from
+    // entry kmax - 1 down; the count word holds both counts (NbrList)
+    int32_t* lp = LIST ? nl.e + (lane == 0 ? (int64_t)0 : (int64_t)(nl.kmax - 1) * nl.stride) + i : nullptr;
+    const int64_t lstep = lane == 0 ? nl.stride : -nl.stride;
     if (LIST) {  // every candidate lies between the first and the last neighbour row
         const int m = S.reach;
         const int zl = DIM == 3 ? max(c[2] - m, 0) : 0, zh = DIM == 3 ? min(c[2] + m, S.n[2] - 1) : 0;
@@ -506,14 +512,15 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         if (LIST) {  // coincident neighbours are listed too: the Shepard sums count them
             if (cnt < nl.kmax) {
                 *lp = (int32_t)(((uint32_t)(j - i) << 9) | (uint32_t)code);
-                lp += nl.stride;
+                lp += lstep;
             } else {
                 list_ok = false;
             }
             ++cnt;
         }
-        if (d2 == 0.f) return;
-        const float inv_r = rsqrtf(d2);
+        // a coincident neighbour (d2 == 0) gets 1/r = 0, hence r = 0, dW = 0 and no
+        // continuity term, without a branch in the walk
+        const float inv_r = d2 > 0.f ? rsqrtf(d2) : 0.f;
         const float r = d2 * inv_r;
         float W, dW;
         kernel_wdw_f<KK>(r * S.inv_h_f, S, W, dW);
@@ -533,10 +540,16 @@ __global__ void k_continuity_f32(const SceneDev* __restrict__ scenes, SortedStat
         drho.add(mj * s * (vx * rx + vy * ry + vz * rz));
     });
     group_combine<TPP>(drho, group_mask<TPP>());
+    int n_back = 0;  // entries of lane 1 (two-lane writer)
+    if (LIST && TPP == 2) {
+        n_back = __shfl_xor_sync(group_mask<TPP>(), cnt, 1);
+        list_ok &= __shfl_xor_sync(group_mask<TPP>(), (int)list_ok, 1) != 0;
+    }
     if (lane != 0) return;
     double dr = drho.value();
     if (LIST) {
-        nl.n[i] = list_ok ? cnt : kListWalk;
+        list_ok &= cnt + n_back <= nl.kmax;
+        nl.n[i] = list_ok ? (cnt | (n_back << 16)) : kListWalk;
     }
     if (bf.n) {  // inlet/outlet buffer neighbours, FP64
         using V = typename VecT<DIM>::T;
@@ -910,7 +923,7 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
     const int block = L.block > 0 ? L.block : 128;
     const int grid = (int)(((int64_t)L.cap * TPP + block - 1) / block);
     if (stage == 0) {
-        if constexpr (!SHEP && (!LIST || TPP == 1))
+        if constexpr (!SHEP && (!LIST || TPP <= 2))
             launch_dep(k_continuity_f32<DIM, KK, TPP, PF, LIST>, grid, block, L.stream, L.scenes, L.st, L.sc, L.cap,
                        L.bf, L.nl);
     } else if (mode == kModeFluidWall) {
@@ -927,13 +940,14 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
 // Lanes code: 1, 2, 4, 8 lanes per particle; -1: one lane with a software-pipelined
 // candidate loop (pays off when few warps are resident, i.e. small scenes).  The cell
 // walks (LIST false) take every code for every stage; with the neighbour list (LIST
-// true) continuity runs one lane (1 or -1) and momentum 1, 2, 4 or -1 lanes.
+// true) continuity runs one or two lanes (1, -1 or 2) and momentum 1, 2, 4 or -1 lanes.
 template <int DIM, int KK, bool LIST, bool SHEP>
 void launch_kk(int stage, const LaunchCtx& L) {
     const int tpp = stage == 0 ? L.tpp_continuity : L.tpp_momentum;
     if constexpr (LIST) {
         if (stage == 0) {
             if (tpp == -1) launch_tpp<DIM, KK, 1, true, true, SHEP>(stage, L.mode, L);
+            else if (tpp == 2) launch_tpp<DIM, KK, 2, false, true, SHEP>(stage, L.mode, L);
             else launch_tpp<DIM, KK, 1, false, true, SHEP>(stage, L.mode, L);
             return;
         }

@@ -320,15 +320,16 @@ int32_t sph_batch_free(SphHandle* h, int64_t* out);
  * and 262,144 wall particles and 262,144 grid cells; larger inputs return SPH_ERR_ARG.
  * The first call in a CUDA context looks up that array's device address and caches it
  * with the context's id (a call from another context, e.g. after cudaDeviceReset, looks
- * it up again): make the first call before any stream capture.  All calls share the array: calls that overlap on the GPU race, so
- * serialise them on one stream.  Errors: sph_last_error(NULL). */
+ * it up again): make the first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them on one stream.  Errors:
+ * sph_last_error(NULL). */
 int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double* x, int64_t n_wall,
                                 const double* wall_x, int64_t* counts, void* stream);
 
 /* Autotuner of the FP32-compensated form: times the continuity and momentum gathers on
  * the current state for every lanes-per-particle count {-1, 1, 2, 4, 8} and block size
  * {64, 128, 256}, and the neighbour-list pair (continuity recording the list with lanes
- * {-1, 1}, momentum reading it with lanes {-1, 1, 2, 4}); keeps the faster of the
+ * {-1, 1, 2}, momentum reading it with lanes {-1, 1, 2, 4}); keeps the faster of the
  * cell-walk and list pairs and rebuilds the step graphs.  out[4] (may be NULL) receives
  * the launch shape (see sph_set_launch_shape).  The fluid state is left unchanged.  No-op
  * for the FP64 form, which keeps one thread per particle so that its summation order is
@@ -336,8 +337,10 @@ int32_t sph_count_pairs_noalloc(const SphParams* params, int64_t n, const double
 int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
 
 /* Momentum lanes code of the neighbour list: SPH_LANES_LIST + t, t in {1, 2, 4, -1}.
- * The continuity gather (one lane per particle) records, in its walk order, every
- * neighbour within r_cut of each particle, and the momentum gather of the same step reads
+ * The continuity gather (one or two lanes per particle) records, in its walk order, every
+ * neighbour within r_cut of each particle (two lanes: each lane its share of the
+ * candidates, lane 0 from the list's first entry up, lane 1 from its last entry down),
+ * and the momentum gather of the same step reads
  * that list with t lanes per particle instead of walking the cells a second time (same
  * pairs: positions do not change between the two gathers).  The list holds about
  * 1.25 x the lattice neighbour count of the finest uploaded spacing per particle
@@ -352,7 +355,7 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * is software-pipelined: loads of the next neighbour overlap the current one's
  * arithmetic; momentum lanes -1 take blocks of at most 256), block in {32, 64, ..., 1024}
  * and a multiple of 32.  Momentum lanes may instead be a neighbour-list code
- * (SPH_LANES_LIST + 1, 2, 4 or -1; continuity lanes 1 or -1 then).  Results of the FP32
+ * (SPH_LANES_LIST + 1, 2, 4 or -1; continuity lanes 1, 2 or -1 then).  Results of the FP32
  * form depend on the lanes codes (the order of the compensated partial sums, and for -1
  * against 1 the compiler's contraction of a*b+c into fused multiply-adds), never on the
  * block size. */

@@ -79,6 +79,43 @@ def test_list_lanes_follow_fp64(pkg, code):
         assert rel(got[k], ref[k]) <= 1e-4, (k, rel(got[k], ref[k]))
 
 
+@pytest.mark.parametrize("name", ["cavity", "dam_break", "lid", "periodic", "inlet_outlet", "dam_break_3d"])
+@pytest.mark.parametrize("code", [LIST - 1, LIST + 1, LIST + 2])
+def test_two_lane_list_writer_reads_like_the_one_lane_list(pkg, name, code):
+    # continuity on two lanes records each particle's list from both ends (lane 0 from the
+    # first entry up, lane 1 from the last down); momentum reads the two segments as one
+    # list: after one step density and position equal the one-lane list's to FP32
+    # summation-order noise, in every solve variant (the first step's velocity is not
+    # compared there: from rest it is a near-zero residual of large pressure terms, which
+    # any change of summation order moves), and over a developed flow (200 steps; the
+    # thermal cavity, which starts at rest, 1,000) the state stays within the form's bar
+    # of the FP64 step
+    s = make(name)
+    one = run(pkg, s, 1, (1, code, 1, 64))
+    two = run(pkg, s, 1, (2, code, 1, 64))
+    assert np.array_equal(two["id"], one["id"])
+    for k in ("rho", "x"):
+        assert rel(two[k], one[k]) <= 1e-6, (name, code, k, rel(two[k], one[k]))
+    steps = 1000 if name == "cavity" else 200
+    ref = run(pkg, s, steps, None, precision=0)
+    got = run(pkg, s, steps, (2, code, 1, 64))
+    assert np.array_equal(got["id"], ref["id"])
+    for k in ("rho", "v", "x"):
+        assert rel(got[k], ref[k]) <= 1e-4, (name, code, k, rel(got[k], ref[k]))
+    assert np.array_equal(got["mass"], ref["mass"])
+
+
+def test_two_lane_lists_that_do_not_fit_walk_the_cells(pkg):
+    # as below, with the two-lane writer: the two segments together overflow the row
+    s = scenes_mod().dam_break_2d(dx=0.03)
+    f = s.fluid
+    f.gap_[:] = 2.0 * f.gap_
+    s = dataclasses.replace(s, fluid=f)
+    walk = run(pkg, s, 30, (2, 1, 1, 128))
+    lst = run(pkg, s, 30, (2, LIST + 1, 1, 128))
+    same_pairs(lst, walk)
+
+
 def test_lists_that_do_not_fit_walk_the_cells(pkg):
     # the list depth follows the uploaded spacing: claiming twice the real spacing sizes
     # it for about a quarter of the real neighbours, so nearly every particle's list
@@ -116,7 +153,8 @@ def test_list_shapes_are_checked(pkg):
     from ethersph_gb300 import _abi
     s = scenes_mod().dam_break_2d(dx=0.05)
     with pkg.Simulation(s.params(precision=1), s.n_fluid, s.n_wall) as sim:
-        for bad in ((2, LIST + 1, 1, 128), (1, LIST + 3, 1, 128), (1, LIST + 8, 1, 128), (1, LIST - 1, 1, 512)):
+        for bad in ((4, LIST + 1, 1, 128), (8, LIST + 2, 1, 128), (1, LIST + 3, 1, 128), (1, LIST + 8, 1, 128),
+                    (1, LIST - 1, 1, 512)):
             with pytest.raises(_abi.SphError) as e:
                 sim.set_launch_shape(*bad)
             assert e.value.code == 1, bad  # SPH_ERR_ARG
