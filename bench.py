@@ -44,10 +44,12 @@ LANES_LIST = 16  # SPH_LANES_LIST: momentum lanes codes >= 15 read the neighbour
 # from ncu --set full --clock-control none (cold L2, as the bench's flushed steps), per
 # launch shape captured (continuity lanes, momentum lanes, block; the third entry of a
 # shape is unused): DRAM bytes read + written, issue-active fraction and FP64-pipe
-# fraction (profiles/gathers_f32_natural_convection_256.md).
+# fraction.
 NCU_256 = {
-    ("-1,18,128", "continuity"): {"traffic": 3.839744e6, "issue_active": 0.437, "fp64_pipe": 0.125},
-    ("-1,18,128", "momentum"): {"traffic": 15.29984e6, "issue_active": 0.358, "fp64_pipe": 0.291},
+    ("2,18,128", "continuity"): {"traffic": 3.839232e6, "issue_active": 0.500, "fp64_pipe": 0.259},
+    ("2,18,128", "momentum"): {"traffic": 16.356096e6, "issue_active": 0.398, "fp64_pipe": 0.297},
+    ("2,18,64", "continuity"): {"traffic": 3.837952e6, "issue_active": 0.492, "fp64_pipe": 0.256},
+    ("2,18,64", "momentum"): {"traffic": 16.35712e6, "issue_active": 0.394, "fp64_pipe": 0.297},
 }
 
 
@@ -470,7 +472,7 @@ def run_ours(args, rank, world, local):
             "issue_frac": ncu["issue_active"] if ncu else None,
             "fp64_pipe_frac": ncu["fp64_pipe"] if ncu else None,
             "limiter": ("FP64 ALU (FP64 at 1/64 of the FP32 rate on GB300)" if args.precision == "fp64" else
-                        "issue/latency: dependent neighbour loads and pair arithmetic on 12-23 warps per SM; "
+                        "issue/latency: dependent neighbour loads and pair arithmetic on 22-24 warps per SM; "
                         "DRAM reads at or below the algorithmic bytes"),
         }
 
