@@ -40,8 +40,8 @@ def merged_walls(scene):
 
 
 def cells_per_cutoff(cell_subdivision: int, precision: int, dim: int) -> int:
-    """The library's cell subdivision (its default: 2 cells per r_cut)."""
-    return cell_subdivision if cell_subdivision else 2
+    """The library's cell subdivision (its default: 3 cells per r_cut)."""
+    return cell_subdivision if cell_subdivision else 3
 
 
 def grid_cells(scene, cell_subdivision: int = 0, precision: int = _abi.PRECISION_FP64) -> int:

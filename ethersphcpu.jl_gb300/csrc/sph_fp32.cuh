@@ -160,10 +160,10 @@ __device__ __forceinline__ float kernel_w_f(float q, const SceneDev& S) {
 // of j's cell from i's cell in metres.
 // A neighbour row whose cells x-m .. x+m do not wrap is one contiguous run of the
 // sorted arrays, [b, e); the cell of a candidate follows from the interior cell
-// boundaries (at most 2m = 4 of them): dx = dx0 + #(boundaries <= j).
+// boundaries (at most 2m = 6 of them): dx = dx0 + #(boundaries <= j).
 struct RowRun {
     int b, e, dx0;
-    int bnd[4];
+    int bnd[6];
 };
 
 __device__ __forceinline__ bool row_run(const SceneDev& S, const int32_t* __restrict__ start, int row, int cx,
@@ -178,7 +178,7 @@ __device__ __forceinline__ bool row_run(const SceneDev& S, const int32_t* __rest
     R.e = __ldg(start + row + x1 + 1);
     R.dx0 = x0 - cx;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 6; ++q) {
         const int cell = x0 + 1 + q;
         R.bnd[q] = cell <= x1 ? __ldg(start + row + cell) : INT_MAX;
     }
@@ -232,7 +232,8 @@ __device__ __forceinline__ bool row_span(const SceneDev& S, const int32_t c[3], 
 }
 
 __device__ __forceinline__ int run_dx(const RowRun& R, int j) {
-    return R.dx0 + (j >= R.bnd[0]) + (j >= R.bnd[1]) + (j >= R.bnd[2]) + (j >= R.bnd[3]);
+    return R.dx0 + (j >= R.bnd[0]) + (j >= R.bnd[1]) + (j >= R.bnd[2]) + (j >= R.bnd[3]) + (j >= R.bnd[4]) +
+           (j >= R.bnd[5]);
 }
 
 // Cell offset of a candidate in metres, and its neighbour-list code (see NbrList).

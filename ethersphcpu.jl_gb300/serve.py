@@ -103,11 +103,13 @@ class Server:
             launch_shape = DEFAULT_LAUNCH_SHAPE
         proto2 = scenes.dam_break_2d(dx=0.05).params(precision=precision)
         proto3 = scenes.dam_break_3d(dx=0.05, tank=(0.4, 0.2, 0.4), column=(0.1, 0.1, 0.2)).params(precision=precision)
+        # cells of r_cut/3 (the library's default grid): a dam-break tank takes about 6.75 cells
+        # per fluid particle in 2D and in 3D
         self.batches = {
             2: Batch.for_budget(proto2, int(budget_bytes * (1.0 - share_3d)), scene_capacity,
-                                cells_per_particle=3.0, walls_per_particle=0.6, lib=lib),
+                                cells_per_particle=6.75, walls_per_particle=0.6, lib=lib),
             3: Batch.for_budget(proto3, int(budget_bytes * share_3d), scene_capacity,
-                                cells_per_particle=2.0, walls_per_particle=3.0, lib=lib),
+                                cells_per_particle=6.75, walls_per_particle=3.0, lib=lib),
         }
         if launch_shape is not None:
             for b in self.batches.values():

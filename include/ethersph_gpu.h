@@ -140,7 +140,7 @@ typedef struct SphParams {
     double domain_hi[3];
 
     int32_t nan_check;      /* 1: sph_step returns SPH_ERR_NAN when a fluid state turns non-finite */
-    int32_t cell_subdivision; /* cells per r_cut along each axis (1 or 2; 0 = 2): finer cells
+    int32_t cell_subdivision; /* cells per r_cut along each axis (1, 2 or 3; 0 = 3): finer cells
                                  visit fewer candidates; the neighbour order, and so the
                                  summation order, depends on it */
 } SphParams;

@@ -305,7 +305,7 @@ double dist2(const double* rv, int dim) {
 
 // Neighbour cells of cell (cx, cy, cz) in visiting order: z, then y, then x, each
 // -m .. +m; cells off the grid are skipped, a periodic x axis wraps.
-constexpr int kMaxCells = 125;  // (2 m + 1)^3 for m = 2
+constexpr int kMaxCells = 343;  // (2 m + 1)^3 for m = 3
 int neighbour_cells(const Grid& G, const int64_t c[3], int64_t out[kMaxCells]) {
     int cnt = 0;
     const int m = G.m;
@@ -1052,9 +1052,9 @@ bool load_model(const SphParams* p, Model* M, Kern* K) {
     M->check_interval = p->check_interval;
     M->check_enabled = p->check_enabled;
     M->periodic_x = p->periodic_x;
-    // the library's default: 2 cells per r_cut
-    M->cells_per_rc = p->cell_subdivision != 0 ? p->cell_subdivision : 2;
-    if (M->cells_per_rc != 1 && M->cells_per_rc != 2) return false;
+    // the library's default: 3 cells per r_cut
+    M->cells_per_rc = p->cell_subdivision != 0 ? p->cell_subdivision : 3;
+    if (M->cells_per_rc < 1 || M->cells_per_rc > 3) return false;
     if (M->periodic_x) {
         const double edge = K->rc * (1.0 + 1e-9) / (double)M->cells_per_rc;
         if (!(std::floor((M->dhi[0] - M->dlo[0]) / edge) >= 2.0 * M->cells_per_rc + 1.0)) return false;

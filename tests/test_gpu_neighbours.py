@@ -99,7 +99,7 @@ CASES = ["dam_break_lattice", "dam_break_jitter", "cavity", "periodic", "dam_bre
          "clamped_2d", "clamped_3d"]
 
 
-@pytest.mark.parametrize("sub", [1, 2])
+@pytest.mark.parametrize("sub", [1, 2, 3])
 @pytest.mark.parametrize("steps", [0, 40])
 @pytest.mark.parametrize("name", CASES)
 def test_fp64_keys_and_neighbour_sets_equal_the_oracle(pkg, orc, name, steps, sub):
