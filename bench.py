@@ -46,10 +46,10 @@ LANES_LIST = 16  # SPH_LANES_LIST: momentum lanes codes >= 15 read the neighbour
 # shape is unused): DRAM bytes read + written, issue-active fraction and FP64-pipe
 # fraction.
 NCU_256 = {
-    ("2,18,128", "continuity"): {"traffic": 3.839232e6, "issue_active": 0.500, "fp64_pipe": 0.259},
-    ("2,18,128", "momentum"): {"traffic": 16.356096e6, "issue_active": 0.398, "fp64_pipe": 0.297},
-    ("2,18,64", "continuity"): {"traffic": 3.837952e6, "issue_active": 0.492, "fp64_pipe": 0.256},
-    ("2,18,64", "momentum"): {"traffic": 16.35712e6, "issue_active": 0.394, "fp64_pipe": 0.297},
+    ("-1,18,128", "continuity"): {"traffic": 3.99616e6, "issue_active": 0.400, "fp64_pipe": 0.145},
+    ("-1,18,128", "momentum"): {"traffic": 15.517184e6, "issue_active": 0.410, "fp64_pipe": 0.304},
+    ("-1,18,64", "continuity"): {"traffic": 3.996416e6, "issue_active": 0.411, "fp64_pipe": 0.142},
+    ("-1,18,64", "momentum"): {"traffic": 15.513856e6, "issue_active": 0.419, "fp64_pipe": 0.300},
 }
 
 
@@ -472,7 +472,7 @@ def run_ours(args, rank, world, local):
             "issue_frac": ncu["issue_active"] if ncu else None,
             "fp64_pipe_frac": ncu["fp64_pipe"] if ncu else None,
             "limiter": ("FP64 ALU (FP64 at 1/64 of the FP32 rate on GB300)" if args.precision == "fp64" else
-                        "issue/latency: dependent neighbour loads and pair arithmetic on 22-24 warps per SM; "
+                        "issue/latency: dependent neighbour loads and pair arithmetic on 13-23 warps per SM; "
                         "DRAM reads at or below the algorithmic bytes"),
         }
 
