@@ -241,6 +241,7 @@ struct SceneRec {
     double gap0 = 0.0;                // gap of the first uploaded fluid particle
     bool uniform_fluid = true;        // every uploaded fluid particle has gap0
     int32_t list_depth = 0;           // neighbour-list entries per particle this scene asks for
+    int64_t n_uploaded = 0;           // fluid particles of the scene's upload (ids 0 .. n - 1)
 };
 
 // First-fit allocator of ranges in [0, cap).
@@ -783,6 +784,17 @@ int32_t add_walls_host(SphHandle* h, SceneRec& R, int32_t kind, int64_t n, const
 
 // Append n fluid particles of scene s at the end of the live range of S[par] (ids
 // 0..n-1 within the scene), then re-sort.
+// Device scratch of downloads and 3D uploads (h->dl_buf) of at least `need` bytes.
+int32_t ensure_dl_buf(SphHandle* h, size_t need) {
+    if (need <= h->dl_cap) return SPH_OK;
+    if (h->dl_buf) cudaFree(h->dl_buf);
+    h->dl_buf = nullptr;
+    h->dl_cap = 0;
+    SPH_CUDA(h, cudaMalloc((void**)&h->dl_buf, need));
+    h->dl_cap = need;
+    return SPH_OK;
+}
+
 int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const double* x, const double* v,
                      const double* rho, const double* p, const double* c, const double* mass, const double* gap,
                      const double* t, const double* kappa, const double* cp) {
@@ -793,45 +805,51 @@ int32_t append_fluid(SphHandle* h, int s, int32_t n_before, int64_t n, const dou
     if (n > 0 && h->thermal && (!t || !kappa || !cp))
         return fail(h, SPH_ERR_ARG, "thermal particles need t, kappa and cp");
     const size_t vb = vec_bytes(dim);
-    std::vector<char> hx(n * vb), hv(n * vb);
-    for (int64_t i = 0; i < n; ++i) {
-        double* px = (double*)(hx.data() + i * vb);
-        double* pv = (double*)(hv.data() + i * vb);
-        for (int k = 0; k < dim; ++k) {
-            px[k] = x[i * dim + k];
-            pv[k] = v[i * dim + k];
-        }
-        if (dim == 3) px[3] = pv[3] = 0.0;
-    }
-    std::vector<double> hp(n), hc(n);
-    for (int64_t i = 0; i < n; ++i) {
-        if (p && c) {
-            hp[i] = p[i];
-            hc[i] = c[i];
-        } else {  // updatePressure! (UpdatePressure.jl:8-16)
+    // p and c from the caller, or updatePressure! (UpdatePressure.jl:8-16) on the host
+    std::vector<double> hp, hc;
+    const double* pp = p;
+    const double* cc = c;
+    if (!(p && c)) {
+        hp.resize(n);
+        hc.resize(n);
+        for (int64_t i = 0; i < n; ++i) {
             const double rr = rho[i] / S.rho0;
             hp[i] = S.b * (host_powi(rr, S.gamma) - 1.0) + S.p0;
             hc[i] = S.c0 * std::sqrt(host_powi(rr, S.gamma - 1));
         }
+        pp = hp.data();
+        cc = hc.data();
     }
     double gmin = 0.0;
     for (int64_t i = 0; i < n; ++i) gmin = (i == 0 || gap[i] < gmin) ? gap[i] : gmin;
     h->scenes[s].list_depth = n > 0 ? list_depth_for(dim, S.rc2, gmin) : 0;
-    std::vector<int32_t> ids(n), scn(n, s);
-    for (int64_t i = 0; i < n; ++i) ids[i] = (int32_t)i;
+    h->scenes[s].n_uploaded = n;
     SortedState& d = h->S[h->par];
     cudaStream_t st = h->stream;
     const size_t o = (size_t)n_before;
+    // every field goes straight from the caller's array to the device (no host copy: on a
+    // GB300 node a pageable copy of a few MB runs at >100 GB/s, a host-side repack at ~20);
+    // 2D positions and velocities are already the state's double2 records, 3D ones are
+    // widened to 32-byte records on the device
     if (n > 0) {
-        SPH_CUDA(h, cudaMemcpyAsync((char*)d.x + o * vb, hx.data(), n * vb, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync((char*)d.v + o * vb, hv.data(), n * vb, cudaMemcpyHostToDevice, st));
+        if (dim == 2) {
+            SPH_CUDA(h, cudaMemcpyAsync((char*)d.x + o * vb, x, n * 16, cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync((char*)d.v + o * vb, v, n * 16, cudaMemcpyHostToDevice, st));
+        } else {
+            if (int32_t rc = ensure_dl_buf(h, (size_t)n * 48); rc != SPH_OK) return rc;
+            double* x3 = (double*)h->dl_buf;
+            double* v3 = x3 + 3 * n;
+            SPH_CUDA(h, cudaMemcpyAsync(x3, x, n * 24, cudaMemcpyHostToDevice, st));
+            SPH_CUDA(h, cudaMemcpyAsync(v3, v, n * 24, cudaMemcpyHostToDevice, st));
+            launch_widen3(st, x3, v3, (char*)d.x + o * vb, (char*)d.v + o * vb, n);
+        }
         SPH_CUDA(h, cudaMemcpyAsync(d.rho + o, rho, n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(d.p + o, hp.data(), n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(d.c + o, hc.data(), n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.p + o, pp, n * 8, cudaMemcpyHostToDevice, st));
+        SPH_CUDA(h, cudaMemcpyAsync(d.c + o, cc, n * 8, cudaMemcpyHostToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(d.m + o, mass, n * 8, cudaMemcpyHostToDevice, st));
         SPH_CUDA(h, cudaMemcpyAsync(d.gap + o, gap, n * 8, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(d.id + o, ids.data(), n * 4, cudaMemcpyHostToDevice, st));
-        SPH_CUDA(h, cudaMemcpyAsync(d.scene + o, scn.data(), n * 4, cudaMemcpyHostToDevice, st));
+        launch_upload_ids(st, d.id + o, d.scene + o, n, s);
+        SPH_CUDA(h, cudaGetLastError());
         if (h->thermal) {
             SPH_CUDA(h, cudaMemcpyAsync(d.T + o, t, n * 8, cudaMemcpyHostToDevice, st));
             SPH_CUDA(h, cudaMemcpyAsync(d.kappa + o, kappa, n * 8, cudaMemcpyHostToDevice, st));
@@ -889,12 +907,19 @@ int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, do
     cudaStream_t st = h->stream;
     const int dim = h->dim;
     const SortedState& d = h->S[h->par];
-    std::vector<int32_t> ids(n), order;
-    SPH_CUDA(h, cudaMemcpyAsync(ids.data(), d.id + b, n * 4, cudaMemcpyDeviceToHost, st));
-    SPH_CUDA(h, cudaStreamSynchronize(st));
-    ascending_id_order(ids, order);
+    // with no particle deleted or created since the upload the ids are a permutation of
+    // 0 .. n-1 and each particle's row is its id; otherwise the rows follow the ascending
+    // ids, ordered on the host
+    const bool permutation = n == h->scenes[s].n_uploaded && !h->has_buffers;
+    std::vector<int32_t> ids, order;
+    if (!permutation) {
+        ids.resize(n);
+        SPH_CUDA(h, cudaMemcpyAsync(ids.data(), d.id + b, n * 4, cudaMemcpyDeviceToHost, st));
+        SPH_CUDA(h, cudaStreamSynchronize(st));
+        ascending_id_order(ids, order);
+    }
     if (ids_out)
-        for (int64_t q = 0; q < n; ++q) ids_out[q] = ids[order[q]];
+        for (int64_t q = 0; q < n; ++q) ids_out[q] = permutation ? q : ids[order[q]];
     const double* srcs[8] = {d.rho, d.p, d.c, d.m, d.gap, d.T, d.kappa, d.cp};
     double* dsts[8] = {rho, p, c, mass, gap, t, kappa, cp};
     DownloadFields F{};
@@ -909,17 +934,15 @@ int32_t download_scene(SphHandle* h, int s, int64_t capacity, int64_t* n_out, do
     if (!F.x && !F.v && F.n == 0) return SPH_OK;
     const size_t cols = (size_t)(F.x + F.v) * dim + (size_t)F.n;
     const size_t need = (size_t)n * 4 + 16 + (size_t)n * cols * 8;
-    if (need > h->dl_cap) {
-        if (h->dl_buf) cudaFree(h->dl_buf);
-        h->dl_buf = nullptr;
-        h->dl_cap = 0;
-        SPH_CUDA(h, cudaMalloc((void**)&h->dl_buf, need));
-        h->dl_cap = need;
-    }
+    if (int32_t rc = ensure_dl_buf(h, need); rc != SPH_OK) return rc;
     int32_t* d_order = (int32_t*)h->dl_buf;
     double* d_out = (double*)(h->dl_buf + (((size_t)n * 4 + 15) / 16) * 16);
-    SPH_CUDA(h, cudaMemcpyAsync(d_order, order.data(), n * 4, cudaMemcpyHostToDevice, st));
-    launch_gather_rows(st, dim, d_order, n, b, d.x, d.v, F, d_out);
+    if (permutation) {
+        launch_scatter_rows(st, dim, d.id, n, b, d.x, d.v, F, d_out);
+    } else {
+        SPH_CUDA(h, cudaMemcpyAsync(d_order, order.data(), n * 4, cudaMemcpyHostToDevice, st));
+        launch_gather_rows(st, dim, d_order, n, b, d.x, d.v, F, d_out);
+    }
     SPH_CUDA(h, cudaGetLastError());
     double* o = d_out;
     if (x) {

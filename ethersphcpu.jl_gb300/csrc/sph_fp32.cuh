@@ -941,14 +941,17 @@ void launch_tpp(int stage, int mode, const LaunchCtx& L) {
 // Lanes code: 1, 2, 4, 8 lanes per particle; -1: one lane with a software-pipelined
 // candidate loop (pays off when few warps are resident, i.e. small scenes).  The cell
 // walks (LIST false) take every code for every stage; with the neighbour list (LIST
-// true) continuity runs one or two lanes (1, -1 or 2) and momentum 1, 2, 4 or -1 lanes.
+// true) continuity runs one or two lanes (1, -1 or 2; the two-lane list writer loads
+// each lane's next candidate ahead, as -1 does: on GB300 5-22% faster than without in
+// 2D and 3D) and momentum 1, 2, 4 or -1 lanes (there two pipelined lanes were 30-60%
+// slower: the prefetched candidate of three float4 costs the occupancy).
 template <int DIM, int KK, bool LIST, bool SHEP>
 void launch_kk(int stage, const LaunchCtx& L) {
     const int tpp = stage == 0 ? L.tpp_continuity : L.tpp_momentum;
     if constexpr (LIST) {
         if (stage == 0) {
             if (tpp == -1) launch_tpp<DIM, KK, 1, true, true, SHEP>(stage, L.mode, L);
-            else if (tpp == 2) launch_tpp<DIM, KK, 2, false, true, SHEP>(stage, L.mode, L);
+            else if (tpp == 2) launch_tpp<DIM, KK, 2, true, true, SHEP>(stage, L.mode, L);
             else launch_tpp<DIM, KK, 1, false, true, SHEP>(stage, L.mode, L);
             return;
         }

@@ -108,6 +108,14 @@ struct DownloadFields {
 // and v (n x dim) when flagged, then one n-array per field.
 void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int64_t n, int32_t b, const void* x,
                         const void* v, const DownloadFields& F, double* out);
+// The same rows when the ids of [b, b + n) are a permutation of 0 .. n-1: row id[b + k]
+// takes sorted particle b + k (no row order needed).
+void launch_scatter_rows(cudaStream_t stream, int dim, const int32_t* id, int64_t n, int32_t b, const void* x,
+                         const void* v, const DownloadFields& F, double* out);
+// Upload helpers: ids 0 .. n-1 and scene s for [id, id + n); 3D positions and velocities
+// (n x 3, device) widened into the state's 32-byte records.
+void launch_upload_ids(cudaStream_t stream, int32_t* id, int32_t* scene, int64_t n, int32_t s);
+void launch_widen3(cudaStream_t stream, const double* x3, const double* v3, void* x, void* v, int64_t n);
 // FP64 reductions: out[0] = sum m, out[1] = sum m|v|^2/2, out[2] = max |v|.
 void launch_stats(const LaunchCtx& L, double* d_partials, double* d_out);
 // Unique fluid pairs (sorted j > i) and fluid-wall pairs within r_cut.

@@ -541,6 +541,71 @@ __global__ void k_gather_rows(const int32_t* __restrict__ order, int64_t n, int3
     for (int f = 0; f < F.n; ++f) o[f * n + q] = F.src[f][k];
 }
 
+// Rows of a download when the scene's ids are a permutation of 0 .. n-1 (no particle
+// deleted or created since the upload): sorted particle b + k goes to row id[b + k], the
+// caller's original order, with no order computed on the host.
+template <int DIM>
+__global__ void k_scatter_rows(const int32_t* __restrict__ id, int64_t n, int32_t b, const void* __restrict__ x,
+                               const void* __restrict__ v, DownloadFields F, double* __restrict__ out) {
+    using V = typename VecT<DIM>::T;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int64_t q = id[b + k];
+    double* o = out;
+    if (F.x) {
+        const V xv = ((const V*)x)[b + k];
+        o[q * DIM] = xv.x;
+        o[q * DIM + 1] = xv.y;
+        if constexpr (DIM == 3) o[q * DIM + 2] = xv.z;
+        o += n * DIM;
+    }
+    if (F.v) {
+        const V vv = ((const V*)v)[b + k];
+        o[q * DIM] = vv.x;
+        o[q * DIM + 1] = vv.y;
+        if constexpr (DIM == 3) o[q * DIM + 2] = vv.z;
+        o += n * DIM;
+    }
+    for (int f = 0; f < F.n; ++f) o[f * n + q] = F.src[f][b + k];
+}
+
+void launch_scatter_rows(cudaStream_t stream, int dim, const int32_t* id, int64_t n, int32_t b, const void* x,
+                         const void* v, const DownloadFields& F, double* out) {
+    const int grid = (int)((n + 255) / 256);
+    if (dim == 2) k_scatter_rows<2><<<grid, 256, 0, stream>>>(id, n, b, x, v, F, out);
+    else k_scatter_rows<3><<<grid, 256, 0, stream>>>(id, n, b, x, v, F, out);
+}
+
+// Upload of fluid particles [o, o + n) of scene s: ids 0 .. n-1 in upload order and the
+// scene index; in 3D the caller's n x 3 positions and velocities (staged on the device)
+// widen to the 32-byte records of the state.
+__global__ void k_upload_ids(int32_t* __restrict__ id, int32_t* __restrict__ scene, int64_t n, int32_t s) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    id[i] = (int32_t)i;
+    scene[i] = s;
+}
+
+__global__ void k_widen3(const double* __restrict__ x3, const double* __restrict__ v3, double4_32a* __restrict__ x,
+                         double4_32a* __restrict__ v, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4_32a a, w;
+    a.x = x3[3 * i]; a.y = x3[3 * i + 1]; a.z = x3[3 * i + 2]; a.w = 0.0;
+    w.x = v3[3 * i]; w.y = v3[3 * i + 1]; w.z = v3[3 * i + 2]; w.w = 0.0;
+    x[i] = a;
+    v[i] = w;
+}
+
+void launch_upload_ids(cudaStream_t stream, int32_t* id, int32_t* scene, int64_t n, int32_t s) {
+    if (n > 0) k_upload_ids<<<(int)((n + 255) / 256), 256, 0, stream>>>(id, scene, n, s);
+}
+
+void launch_widen3(cudaStream_t stream, const double* x3, const double* v3, void* x, void* v, int64_t n) {
+    if (n > 0)
+        k_widen3<<<(int)((n + 255) / 256), 256, 0, stream>>>(x3, v3, (double4_32a*)x, (double4_32a*)v, n);
+}
+
 void launch_gather_rows(cudaStream_t stream, int dim, const int32_t* order, int64_t n, int32_t b, const void* x,
                         const void* v, const DownloadFields& F, double* out) {
     const int grid = (int)((n + 255) / 256);
