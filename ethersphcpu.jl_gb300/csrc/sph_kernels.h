@@ -37,7 +37,7 @@ struct LaunchCtx {
     // launch shape of the FP32 gathers (lanes per particle, threads per block)
     int block;
     int tpp_continuity, tpp_momentum;
-    // list_momentum != 0: continuity (one lane) records the neighbour list and momentum
+    // list_momentum != 0: continuity (one or two lanes) records the neighbour list and momentum
     // reads it (tpp_momentum lanes per particle)
     int list_momentum;
     NbrList nl;
