@@ -41,7 +41,9 @@ __global__ void k_neighbours_fp64(const SceneDev* __restrict__ scenes, SortedSta
     cell_of<DIM>(xi, S, c);
     int32_t* out = ids ? ids + rows[i - b] : nullptr;
     int32_t cnt = 0;
-    walk_cells<DIM>(S, start, c, [&](int jb, int je) {
+    float xd[3];
+    cell_units<DIM>(xi, S, c, xd);
+    walk_cells_pruned<DIM>(S, start, c, xd, [&](int jb, int je) {
         for (int j = jb; j < je; ++j) {
             if (j == i) continue;
             double rv[DIM];

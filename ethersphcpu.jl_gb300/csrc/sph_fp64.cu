@@ -42,8 +42,10 @@ __global__ void __launch_bounds__(128) k_continuity_fp64(const SceneDev* __restr
     const V vi = v[i];
     int32_t c[3];
     cell_of<DIM>(xi, S, c);
+    float xd[3];
+    cell_units<DIM>(xi, S, c, xd);
     double drho = 0.0;
-    walk_cells<DIM>(S, start, c, [&](int jb, int je) {
+    walk_cells_pruned<DIM>(S, start, c, xd, [&](int jb, int je) {
         for (int j = jb; j < je; ++j) {
             if (j == i) continue;
             const V xj = x[j];
@@ -140,6 +142,8 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
     const double Wg_i = kernel_w<KK>(gap_i, S);
     int32_t c[3];
     cell_of<DIM>(xi, S, c);
+    float xd[3];
+    cell_units<DIM>(xi, S, c, xd);
     double dv[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; ++k) dv[k] = 0.0;
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
     double sw = 0.0, sws = 0.0;
 
     // ---- fluid neighbours: pressureForce! + viscosityForce! (+ thermalConduction!)
-    walk_cells<DIM>(S, sc.start, c, [&](int jb, int je) {
+    walk_cells_pruned<DIM>(S, sc.start, c, xd, [&](int jb, int je) {
         for (int j = jb; j < je; ++j) {
             if (j == i) continue;
             const V xj = x[j];
@@ -238,7 +242,7 @@ __global__ void __launch_bounds__(128) k_momentum_fp64(const SceneDev* __restric
         const V* __restrict__ wn = (const V*)wl.nrm;
         const V* __restrict__ wv = (const V*)wl.v;
         const double Wgap_bg = Wg_i;  // kernelValue(p_i.gap_) of PressureForce.jl:30
-        walk_cells<DIM>(S, wl.start, c, [&](int jb, int je) {
+        walk_cells_pruned<DIM>(S, wl.start, c, xd, [&](int jb, int je) {
             for (int w = jb; w < je; ++w) {
                 const V xw = wx[w];
                 double rv[DIM];

@@ -197,6 +197,78 @@ __device__ __forceinline__ void walk_cells(const SceneDev& S, const int32_t* __r
     }
 }
 
+// The same walk for the gathers of the FP64 form, with stencil pruning: in each neighbour
+// row only the x cells whose extent comes within r_cut of the particle are visited, and a
+// row whose y (and z) extent lies beyond r_cut is skipped.  fu is the particle's position
+// in cell units relative to its cell c (FP32: the bounds cost a few FP32 operations a row,
+// where FP64 work is 64 times slower on GB300), and the test keeps a relative margin of
+// 1e-4 on r_cut^2, far above the FP32 rounding of positions within a few cells.  Only
+// candidates the distance test would reject are left out, in a walk that keeps the order
+// of the others: the sums are bitwise those of walk_cells.  Rows on the y/z grid boundary
+// and the grid's first and last x cells may hold particles clamped from outside the grid
+// (beyond their cell's extent) and are never trimmed; a periodic axis is walked whole.
+template <int DIM, typename F>
+__device__ __forceinline__ void walk_cells_pruned(const SceneDev& S, const int32_t* __restrict__ start,
+                                                  const int32_t c[3], const float fu[3], F&& f) {
+    if (S.periodic_x) {
+        walk_cells<DIM>(S, start, c, f);
+        return;
+    }
+    const int m = S.reach;
+    const int zr = DIM == 3 ? m : 0;
+    const float r2 = S.rc2_f * 1.0001f;
+    const float ey = S.cell_f[1], ez = S.cell_f[2];
+    const float inv_ex = S.inv_cell_fx;
+    for (int dz = -zr; dz <= zr; ++dz) {
+        const int z = c[2] + dz;
+        if (DIM == 3 && (z < 0 || z >= S.n[2])) continue;
+        float gz2 = 0.f;
+        if (DIM == 3 && z > 0 && z < S.n[2] - 1) {
+            const float gz = fmaxf(fmaxf((float)dz - fu[2], fu[2] - (float)(dz + 1)), 0.f) * ez;
+            gz2 = gz * gz;
+        }
+        for (int dy = -m; dy <= m; ++dy) {
+            const int y = c[1] + dy;
+            if (y < 0 || y >= S.n[1]) continue;
+            const int row = S.cell_off + (z * S.n[1] + y) * S.n[0];
+            int x0 = c[0] > m ? c[0] - m : 0;
+            int x1 = c[0] + m < S.n[0] ? c[0] + m : S.n[0] - 1;
+            const bool edge_row = y == 0 || y == S.n[1] - 1 || (DIM == 3 && (z == 0 || z == S.n[2] - 1));
+            if (!edge_row) {
+                const float gy = fmaxf(fmaxf((float)dy - fu[1], fu[1] - (float)(dy + 1)), 0.f) * ey;
+                const float rem = r2 - (gy * gy + gz2);
+                if (rem < 0.f) continue;
+                const float wu = sqrtf(rem) * inv_ex;  // half-width in x cells
+                // cells entirely left of x - w or right of x + w hold no candidate within
+                // r_cut; the grid's first and last cells stay when the stencil reaches them
+                const bool keep_first = x0 == 0, keep_last = x1 == S.n[0] - 1;
+                int a = x0, e = x1;
+                const int al = c[0] + (int)floorf(fu[0] - wu), eh = c[0] + (int)floorf(fu[0] + wu);
+                if (!keep_first && al > a) a = al < x1 + 1 ? al : x1 + 1;
+                if (!keep_last && eh < e) e = eh > x0 - 1 ? eh : x0 - 1;
+                if (keep_first && e < 0) e = 0;
+                if (keep_last && a > S.n[0] - 1) a = S.n[0] - 1;
+                if (a > e) continue;
+                x0 = a;
+                x1 = e;
+            }
+            f(__ldg(start + row + x0), __ldg(start + row + x1 + 1));
+        }
+    }
+}
+
+// The position of x in cell units relative to its cell c (FP64 once, then FP32 for the
+// pruning bounds of walk_cells_pruned).
+template <int DIM, typename V>
+__device__ __forceinline__ void cell_units(const V& x, const SceneDev& S, const int32_t c[3], float fu[3]) {
+    // a particle clamped from far outside the grid keeps a bounded value (the pruning
+    // decisions are the same for any distance beyond the stencil)
+    fu[0] = (float)fmin(fmax((x.x - S.lo[0]) * S.inv_cell[0] - (double)c[0], -1e6), 1e6);
+    fu[1] = (float)fmin(fmax((x.y - S.lo[1]) * S.inv_cell[1] - (double)c[1], -1e6), 1e6);
+    fu[2] = DIM == 3 ? (float)fmin(fmax((comp(x, DIM - 1) - S.lo[2]) * S.inv_cell[2] - (double)c[2], -1e6), 1e6)
+                     : 0.f;
+}
+
 template <int DIM, typename V>
 __device__ __forceinline__ void cell_of(const V& x, const SceneDev& S, int32_t c[3]) {
     c[0] = cell_coord(x.x, S, 0);

@@ -361,7 +361,8 @@ int32_t sph_autotune(SphHandle* h, int32_t reps, int32_t* out);
  * block size. */
 int32_t sph_set_launch_shape(SphHandle* h, const int32_t* shape);
 
-/* Stencil pruning of the FP32-compensated walks (default: on for 3D scenes, off for 2D,
+/* Stencil pruning of the FP32-compensated walks (the FP64 form's walks always prune, with
+ * the same bitwise-neutral rule; default: on for 3D scenes, off for 2D,
  * where it does not pay on GB300): for each neighbour row
  * the walk visits only the cells whose extent comes within r_cut of the particle (with a
  * margin of 1e-5 on r_cut^2), instead of all 2m+1 cells of the (2m+1)^dim stencil.  Only
